@@ -1,0 +1,378 @@
+// Truncated SVD on the device: one-sided (Hestenes) cyclic Jacobi in FP64.
+//
+// The columns of a working copy X (r x c, column-major, c = min(m, n)) are
+// orthogonalised pairwise with the round-robin (tournament) ordering, so the
+// c/2 pairs of a round touch disjoint columns and run concurrently, one warp
+// per pair: the warp reduces the 2x2 Gram block (|x_p|^2, |x_q|^2,
+// x_p^H x_q) with shuffles, builds the Hermitian Jacobi rotation and applies
+// it to the two columns of X and of the accumulated V.  Rounds are separated
+// by a barrier: __syncthreads() for the single-CTA variant (small matrices,
+// the common case at the chain edges and at small chi) or a bounded grid
+// barrier for the cooperative multi-CTA variant.  A sweep with no rotation
+// above tol*sqrt(|x_p|^2 |x_q|^2) ends the iteration.  The singular values
+// are the column norms of X; the singular vectors are X/sigma and V.  Unlike
+// the Gram-matrix route this keeps small singular values to high relative
+// accuracy, so no exact-SVD fallback is needed.
+#include "common.cuh"
+
+namespace dmrg {
+
+namespace {
+
+constexpr long long kBarrierSpinLimit = 1ll << 26;  // ~seconds: far beyond any real wait
+
+struct GridBar {
+  unsigned* count;
+  unsigned* gen;
+  int* err;
+};
+
+// Bounded grid-wide barrier for cooperatively launched grids (all CTAs
+// co-resident).  Gives up after kBarrierSpinLimit polls, records
+// DMRG_ERR_TIMEOUT and lets every CTA fall through.
+__device__ __forceinline__ bool grid_barrier(const GridBar& b) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = b.gen;
+    unsigned g = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(b.count, 1u);
+    if (arrived == gridDim.x - 1) {
+      *b.count = 0u;
+      __threadfence();
+      atomicAdd(b.gen, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == g) {
+        if (++it > kBarrierSpinLimit) {
+          atomicExch(b.err, DMRG_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *((volatile int*)b.err) == 0;
+}
+
+template <typename T>
+struct HArgs {
+  T* X;          // r x c, column-major (ld = r)
+  T* V;          // c x c, column-major (ld = c)
+  int r, c, cp;  // cp = c rounded up to even
+  int max_sweeps;
+  double tol;
+  GridBar bar;
+  unsigned* rotcnt;  // [3], used cyclically: sweep k counts into slot k%3
+  int* sweeps_out;
+};
+
+template <typename T>
+__device__ __forceinline__ void gram2(const T* xp, const T* xq, int r, int lane, double& al, double& be, double& gre,
+                                      double& gim);
+template <>
+__device__ __forceinline__ void gram2<double>(const double* xp, const double* xq, int r, int lane, double& al,
+                                              double& be, double& gre, double& gim) {
+  al = be = gre = gim = 0.0;
+  for (int i = lane; i < r; i += 32) {
+    double a = xp[i], b = xq[i];
+    al = ::fma(a, a, al);
+    be = ::fma(b, b, be);
+    gre = ::fma(a, b, gre);
+  }
+}
+template <>
+__device__ __forceinline__ void gram2<cplx>(const cplx* xp, const cplx* xq, int r, int lane, double& al, double& be,
+                                            double& gre, double& gim) {
+  al = be = gre = gim = 0.0;
+  for (int i = lane; i < r; i += 32) {
+    cplx a = xp[i], b = xq[i];
+    al = ::fma(a.x, a.x, ::fma(a.y, a.y, al));
+    be = ::fma(b.x, b.x, ::fma(b.y, b.y, be));
+    gre = ::fma(a.x, b.x, ::fma(a.y, b.y, gre));   // Re conj(a) b
+    gim = ::fma(a.x, b.y, ::fma(-a.y, b.x, gim));  // Im conj(a) b
+  }
+}
+
+// apply X <- X J on columns (p, q): J = [[c, s e], [-s conj(e), c]]
+template <typename T>
+__device__ __forceinline__ void rot_cols(T* xp, T* xq, int r, int lane, double c, double s, T e) {
+  const T se = Sc<T>::scale(e, s);
+  const T sce = Sc<T>::scale(Sc<T>::conj(e), s);
+  for (int i = lane; i < r; i += 32) {
+    T a = xp[i], b = xq[i];
+    xp[i] = Sc<T>::sub(Sc<T>::scale(a, c), Sc<T>::mul(sce, b));
+    xq[i] = Sc<T>::add(Sc<T>::mul(se, a), Sc<T>::scale(b, c));
+  }
+}
+
+__device__ __forceinline__ int player(int pos, int round, int cp) {
+  return pos == 0 ? 0 : 1 + (pos - 1 + round) % (cp - 1);
+}
+
+template <typename T, bool COOP>
+__global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int half = a.cp / 2;
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+
+  // V = identity
+  for (long long idx = gtid; idx < (long long)a.c * a.c; idx += gthreads) {
+    int col = (int)(idx / a.c), row = (int)(idx - (long long)col * a.c);
+    a.V[idx] = row == col ? Sc<T>::one() : Sc<T>::zero();
+  }
+  if (gtid == 0) { a.rotcnt[0] = 0u; a.rotcnt[1] = 0u; a.rotcnt[2] = 0u; }
+  if (COOP) { if (!grid_barrier(a.bar)) return; } else { __syncthreads(); }
+
+  int sweep = 0;
+  bool converged = a.cp < 2;
+  for (; sweep < a.max_sweeps && !converged; ++sweep) {
+    // slot (sweep+1)%3 was last read at the end of sweep-2, before at least
+    // one barrier of sweep-1, so no CTA can still be reading it
+    if (gtid == 0) a.rotcnt[(sweep + 1) % 3] = 0u;
+    for (int round = 0; round < a.cp - 1; ++round) {
+      for (int i = gw; i < half; i += nw) {
+        int p = player(i, round, a.cp), q = player(a.cp - 1 - i, round, a.cp);
+        if (p > q) { int t = p; p = q; q = t; }
+        if (q >= a.c) continue;  // dummy column of an odd count
+        T* xp = a.X + (long long)p * a.r;
+        T* xq = a.X + (long long)q * a.r;
+        double al, be, gre, gim;
+        gram2<T>(xp, xq, a.r, lane, al, be, gre, gim);
+        al = warp_sum(al);
+        be = warp_sum(be);
+        gre = warp_sum(gre);
+        gim = warp_sum(gim);
+        double ag = sqrt(gre * gre + gim * gim);
+        double scale = sqrt(al * be);
+        if (!(ag > a.tol * scale) || !(ag > 1e-300)) continue;
+        double tau = (be - al) / (2.0 * ag);
+        double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        double cs = 1.0 / sqrt(1.0 + t * t);
+        double sn = t * cs;
+        T e = Sc<T>::make(gre / ag, gim / ag);
+        rot_cols<T>(xp, xq, a.r, lane, cs, sn, e);
+        rot_cols<T>(a.V + (long long)p * a.c, a.V + (long long)q * a.c, a.c, lane, cs, sn, e);
+        if (lane == 0) atomicAdd(&a.rotcnt[sweep % 3], 1u);
+      }
+      if (COOP) { if (!grid_barrier(a.bar)) return; } else { __syncthreads(); }
+    }
+    converged = (((volatile unsigned*)a.rotcnt)[sweep % 3] == 0u);
+  }
+  if (gtid == 0) *a.sweeps_out = converged ? sweep : -sweep;
+}
+
+// sigma_j = |X_j|, one warp per column
+template <typename T>
+__global__ void colnorm_kernel(const T* __restrict__ X, int r, int c, double* __restrict__ sig) {
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= c) return;
+  const T* x = X + (long long)w * r;
+  double s = 0.0;
+  for (int i = lane; i < r; i += 32) s += Sc<T>::abs2(x[i]);
+  s = warp_sum(s);
+  if (lane == 0) sig[w] = sqrt(s);
+}
+
+// perm[k] = index of the k-th largest sigma (stable), sorted[k] = its value
+__global__ void rank_kernel(const double* __restrict__ sig, int c, int* __restrict__ perm, double* __restrict__ sorted) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c) return;
+  double v = sig[i];
+  int rank = 0;
+  for (int j = 0; j < c; ++j) {
+    double u = sig[j];
+    rank += (u > v) || (u == v && j < i);
+  }
+  perm[rank] = i;
+  sorted[rank] = v;
+}
+
+// copy M (row-major m x n) into X (column-major r x c):
+//   left = (m <= n): X = M^H  (r = n, c = m): X[j*n + i] = conj(M[j*n + i])
+//   else           : X = M    (r = m, c = n): X[j*m + i] = M[i*n + j]
+template <typename T>
+__global__ void load_x_kernel(const T* __restrict__ M, int m, int n, int left, T* __restrict__ X) {
+  long long total = (long long)m * n;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += stride) {
+    if (left) {
+      X[idx] = Sc<T>::conj(M[idx]);
+    } else {
+      int j = (int)(idx / m), i = (int)(idx - (long long)j * m);
+      X[idx] = M[(long long)i * n + j];
+    }
+  }
+}
+
+// Outputs.  left case (X = M^H V = Y, U = V, S.Vh = Y^H):
+//   lo[i,k] = V[i, perm k] * (absorb==1 ? sigma_k : 1)           (m x keep)
+//   ro[k,j] = conj(Y[j, perm k]) / (absorb==0 ? 1 : sigma_k)     (keep x n)
+// right case (X = M V = Y, U = Y/sigma, Vh = V^H):
+//   lo[i,k] = Y[i, perm k] / (absorb==1 ? 1 : sigma_k)
+//   ro[k,j] = conj(V[j, perm k]) * (absorb==0 ? sigma_k : 1)
+template <typename T>
+__global__ void out_kernel(const T* __restrict__ X, const T* __restrict__ V, const int* __restrict__ perm,
+                           const double* __restrict__ sorted, int m, int n, int left, int keep, int absorb,
+                           T* __restrict__ lo, T* __restrict__ ro) {
+  long long nl = (long long)m * keep, nr = (long long)keep * n;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < nl + nr; idx += stride) {
+    if (idx < nl) {
+      int i = (int)(idx / keep), k = (int)(idx - (long long)i * keep);
+      int pk = perm[k];
+      double sg = sorted[k];
+      T v;
+      if (left) {
+        v = V[(long long)pk * m + i];
+        if (absorb == 1) v = Sc<T>::scale(v, sg);
+      } else {
+        v = X[(long long)pk * m + i];
+        if (absorb != 1) v = Sc<T>::scale(v, sg > 0.0 ? 1.0 / sg : 0.0);
+      }
+      lo[idx] = v;
+    } else {
+      long long o = idx - nl;
+      int k = (int)(o / n), j = (int)(o - (long long)k * n);
+      int pk = perm[k];
+      double sg = sorted[k];
+      T v;
+      if (left) {
+        v = Sc<T>::conj(X[(long long)pk * n + j]);
+        if (absorb != 0) v = Sc<T>::scale(v, sg > 0.0 ? 1.0 / sg : 0.0);
+      } else {
+        v = Sc<T>::conj(V[(long long)pk * n + j]);
+        if (absorb == 0) v = Sc<T>::scale(v, sg);
+      }
+      ro[o] = v;
+    }
+  }
+}
+
+inline int egrid(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+}  // namespace
+
+struct SvdWork {
+  void* X;
+  void* V;
+  double* sig;
+  double* sorted;
+  int* perm;
+  unsigned* ctrl;  // [0..1] barrier, [2..4] rotation counters, [5] err, [6] sweeps
+};
+
+size_t svd_work_bytes(int dtype, int m, int n) {
+  size_t es = dtype == DMRG_COMPLEX128 ? 16 : 8;
+  size_t c = (size_t)(m < n ? m : n);
+  size_t r = (size_t)(m < n ? n : m);
+  return align_up(r * c * es) + align_up(c * c * es) + 2 * align_up(c * 8) + align_up(c * 4) + align_up(64);
+}
+
+static SvdWork carve(void* work, int dtype, int m, int n) {
+  size_t es = dtype == DMRG_COMPLEX128 ? 16 : 8;
+  size_t c = (size_t)(m < n ? m : n);
+  size_t r = (size_t)(m < n ? n : m);
+  char* p = static_cast<char*>(work);
+  SvdWork w;
+  w.X = p; p += align_up(r * c * es);
+  w.V = p; p += align_up(c * c * es);
+  w.sig = reinterpret_cast<double*>(p); p += align_up(c * 8);
+  w.sorted = reinterpret_cast<double*>(p); p += align_up(c * 8);
+  w.perm = reinterpret_cast<int*>(p); p += align_up(c * 4);
+  w.ctrl = reinterpret_cast<unsigned*>(p);
+  return w;
+}
+
+// Phase 1: factorise.  Leaves sorted singular values in w.sorted (device)
+// and copies them to host_s.  Returns DMRG_ERR_NOCONV if the sweep limit was
+// reached (the factorisation is still usable).
+template <typename T>
+int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, cudaStream_t s) {
+  const int left = m <= n;
+  const int r = left ? n : m;
+  const int c = left ? m : n;
+  SvdWork w = carve(work, sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64, m, n);
+  DMRG_CUDA_TRY(cudaMemsetAsync(w.ctrl, 0, 64, s));
+  load_x_kernel<T><<<egrid((long long)m * n), 256, 0, s>>>(M, m, n, left, static_cast<T*>(w.X));
+  DMRG_CHECK_LAUNCH();
+  HArgs<T> a;
+  a.X = static_cast<T*>(w.X);
+  a.V = static_cast<T*>(w.V);
+  a.r = r;
+  a.c = c;
+  a.cp = c + (c & 1);
+  a.max_sweeps = 60;
+  double tol = 2.2e-16 * sqrt((double)r);
+  a.tol = tol > 1e-15 ? tol : 1e-15;
+  a.bar.count = w.ctrl + 0;
+  a.bar.gen = w.ctrl + 1;
+  a.rotcnt = w.ctrl + 2;
+  a.bar.err = reinterpret_cast<int*>(w.ctrl + 5);
+  a.sweeps_out = reinterpret_cast<int*>(w.ctrl + 6);
+  const int half = a.cp / 2;
+  // one CTA while the pairs of a round fit in 32 warps of one CTA and the
+  // columns are short; otherwise a cooperative grid with one warp per pair
+  if ((half <= 64 && (long long)r * c <= (1ll << 20)) || half <= 8) {
+    int threads = 32 * (half < 32 ? (half > 0 ? half : 1) : 32);
+    hestenes_kernel<T, false><<<1, threads, 0, s>>>(a);
+    DMRG_CHECK_LAUNCH();
+  } else {
+    int dev = 0;
+    DMRG_CUDA_TRY(cudaGetDevice(&dev));
+    int nsm = 0;
+    DMRG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    int per_sm = 0;
+    const int threads = 256;
+    DMRG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hestenes_kernel<T, true>, threads, 0));
+    if (per_sm < 1) return DMRG_ERR_CUDA;
+    int want = (half + (threads / 32) - 1) / (threads / 32);
+    int maxb = per_sm * nsm;
+    int blocks = want < maxb ? want : maxb;
+    if (blocks < 1) blocks = 1;
+    void* args[] = {&a};
+    DMRG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)hestenes_kernel<T, true>, blocks, threads, args, 0, s));
+  }
+  colnorm_kernel<T><<<(c * 32 + 255) / 256, 256, 0, s>>>(a.X, r, c, w.sig);
+  DMRG_CHECK_LAUNCH();
+  rank_kernel<<<(c + 255) / 256, 256, 0, s>>>(w.sig, c, w.perm, w.sorted);
+  DMRG_CHECK_LAUNCH();
+  int ctrl_host[2] = {0, 0};
+  DMRG_CUDA_TRY(cudaMemcpyAsync(host_s, w.sorted, sizeof(double) * c, cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaMemcpyAsync(ctrl_host, w.ctrl + 5, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (ctrl_host[0] != 0) return ctrl_host[0];
+  if (sweeps) *sweeps = ctrl_host[1];
+  for (int k = 0; k < c; ++k)
+    if (!(host_s[k] == host_s[k]) || host_s[k] > 1e300) return DMRG_ERR_NAN;
+  return ctrl_host[1] < 0 ? DMRG_ERR_NOCONV : DMRG_OK;
+}
+
+template <typename T>
+int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s) {
+  const int left = m <= n;
+  SvdWork w = carve(work, sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64, m, n);
+  long long tot = (long long)m * keep + (long long)keep * n;
+  out_kernel<T><<<egrid(tot), 256, 0, s>>>(static_cast<const T*>(w.X), static_cast<const T*>(w.V), w.perm, w.sorted,
+                                           m, n, left, keep, absorb, lo, ro);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+template int hestenes_factor<double>(const double*, int, int, void*, double*, int*, cudaStream_t);
+template int hestenes_factor<cplx>(const cplx*, int, int, void*, double*, int*, cudaStream_t);
+template int hestenes_output<double>(int, int, int, int, void*, double*, double*, cudaStream_t);
+template int hestenes_output<cplx>(int, int, int, int, void*, cplx*, cplx*, cudaStream_t);
+
+}  // namespace dmrg

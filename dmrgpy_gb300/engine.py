@@ -1,0 +1,415 @@
+"""Device-resident two-site DMRG / TDVP sweep driven through the C ABI.
+
+The host loop mirrors the reference sweep structure
+(``pyitensor/dmrg.py:355-398`` for DMRG, ``pyitensor/tdvp.py:220-368`` for
+TDVP); every numerical step -- two-site merge, H_eff matvec, Lanczos /
+Krylov-exponential loops, truncated SVD, environment extension -- runs as
+CUDA kernels of libdmrg_gb300.so on tensors that stay in HBM.  PyTorch only
+provides device memory and the stream.  There is no CPU fallback: without a
+CUDA device the engine refuses to start.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from . import _lib
+
+LANCZOS_TOL = 1e-12          # pyitensor/dmrg.py:95
+LANCZOS_NITER_FLOOR = 200    # pyitensor/dmrg.py:315-330
+KRYLOV_ERRGOAL = 1e-10       # pyitensor/tdvp.py:79
+KRYLOV_TOL = 1e-12           # pyitensor/tdvp.py:82
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Workspace:
+    """One growing device scratch buffer shared by all entry points (calls
+    are stream-ordered, so reuse is safe)."""
+
+    def __init__(self, device):
+        self.device = device
+        self.buf = None
+
+    def get(self, nbytes):
+        torch = _torch()
+        nbytes = int(max(nbytes, 256))
+        if self.buf is None or self.buf.numel() < nbytes:
+            self.buf = None
+            self.buf = torch.empty(int(nbytes * 1.25) + 4096, dtype=torch.uint8, device=self.device)
+        return self.buf.data_ptr(), self.buf.numel()
+
+
+class SweepStats:
+    def __init__(self):
+        self.records = []
+        self.t = {"lanczos": 0.0, "svd": 0.0, "env": 0.0, "merge": 0.0}
+        self.matvecs = 0
+        self.matvec_flops = 0.0
+
+    def add(self, **kw):
+        self.records.append(kw)
+
+
+class Engine:
+    """Sweeps over an MPO held on the device.
+
+    W: list of (w_left, d, d, w_right) numpy arrays; real: element type.
+    precision: "fp64" or "tf32x3" (split-TF32 contractions, real only).
+    """
+
+    def __init__(self, W, real=True, precision="fp64", device="cuda:0", krylov_budget_bytes=32 << 30):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("dmrgpy_gb300 needs a CUDA device (GB300); no CPU fallback exists")
+        self.lib = _lib.load()
+        self.device = torch.device(device)
+        self.real = bool(real)
+        self.tdtype = torch.float64 if self.real else torch.complex128
+        self.cdtype = _lib.REAL64 if self.real else _lib.COMPLEX128
+        self.esize = 8 if self.real else 16
+        if precision not in ("fp64", "tf32x3"):
+            raise ValueError("precision must be 'fp64' or 'tf32x3'")
+        if precision == "tf32x3" and not self.real:
+            raise ValueError("tf32x3 contractions are built for real MPOs only")
+        self.precision = precision
+        self.prec = _lib.PREC_FP64 if precision == "fp64" else _lib.PREC_TF32X3
+        self.W = [torch.as_tensor(np.ascontiguousarray(w, dtype=np.float64 if self.real else np.complex128),
+                                  device=self.device) for w in W]
+        self.n = len(W)
+        self.ws = Workspace(self.device)
+        self.edge = torch.ones((1, 1, 1), dtype=self.tdtype, device=self.device)
+        self.krylov_budget = krylov_budget_bytes
+        self.stats = SweepStats()
+        self._renv = None  # right environments valid for the current MPS (after a RL pass)
+
+    # ------------------------------------------------------------ plumbing
+    @property
+    def stream(self):
+        return ctypes.c_void_p(_torch().cuda.current_stream(self.device).cuda_stream)
+
+    def to_device(self, arrays):
+        torch = _torch()
+        out = []
+        for a in arrays:
+            a = np.asarray(a)
+            if self.real:
+                a = a.real if np.iscomplexobj(a) else a
+                a = np.ascontiguousarray(a, dtype=np.float64)
+            else:
+                a = np.ascontiguousarray(a, dtype=np.complex128)
+            out.append(torch.as_tensor(a, device=self.device))
+        return out
+
+    def to_host(self, tensors):
+        return [t.detach().cpu().numpy() for t in tensors]
+
+    def _heff(self, kind, L, W1, W2, R, cl, d1, d2, cr, wl, wm, wr):
+        h = _lib.HeffDesc()
+        h.kind, h.dtype, h.precision = kind, self.cdtype, self.prec
+        h.chil, h.d1, h.d2, h.chir = cl, d1, d2, cr
+        h.wl, h.wm, h.wr = wl, wm, wr
+        h.L = L.data_ptr()
+        h.R = R.data_ptr()
+        h.W1 = W1.data_ptr() if W1 is not None else None
+        h.W2 = W2.data_ptr() if W2 is not None else None
+        return h
+
+    def heff2(self, L, Wi, Wj, R, theta_shape):
+        cl, d1, d2, cr = theta_shape
+        return self._heff(2, L, Wi, Wj, R, cl, d1, d2, cr, Wi.shape[0], Wi.shape[3], Wj.shape[3])
+
+    def heff1(self, L, W, R, a_shape):
+        cl, d, cr = a_shape
+        return self._heff(1, L, W, None, R, cl, d, 1, cr, W.shape[0], W.shape[3], W.shape[3])
+
+    def heff0(self, L, R, c_shape):
+        cl, cr = c_shape
+        w = L.shape[1]
+        return self._heff(0, L, None, None, R, cl, 1, 1, cr, w, w, w)
+
+    def apply(self, h, x):
+        """y = H_eff x (one matvec; used by tests and the benchmark)."""
+        torch = _torch()
+        y = torch.empty_like(x)
+        need = self.lib.dmrg_heff_workspace_bytes(ctypes.byref(h))
+        ptr, size = self.ws.get(need)
+        _lib.check("dmrg_heff_apply", self.lib.dmrg_heff_apply(ctypes.byref(h), x.data_ptr(), y.data_ptr(),
+                                                                 ptr, size, self.stream))
+        return y
+
+    def _kcap(self, n, niter):
+        cap = max(8, int(self.krylov_budget // max(1, n * self.esize)))
+        return int(min(niter, cap))
+
+    def ground(self, h, x, niter):
+        """Lowest eigenpair of H_eff; x (contiguous) is overwritten by the
+        normalised eigenvector."""
+        k = self._kcap(x.numel(), max(niter, LANCZOS_NITER_FLOOR))
+        need = self.lib.dmrg_lanczos_workspace_bytes(ctypes.byref(h), k)
+        ptr, size = self.ws.get(need)
+        e = ctypes.c_double(0.0)
+        it = ctypes.c_int(0)
+        _lib.check("dmrg_lanczos_ground", self.lib.dmrg_lanczos_ground(
+            ctypes.byref(h), x.data_ptr(), k, LANCZOS_TOL, ctypes.byref(e), ctypes.byref(it), ptr, size, self.stream))
+        return e.value, it.value
+
+    def expm(self, h, x, coeff, niter):
+        k = self._kcap(x.numel(), niter)
+        need = self.lib.dmrg_expm_workspace_bytes(ctypes.byref(h), k)
+        ptr, size = self.ws.get(need)
+        it = ctypes.c_int(0)
+        coeff = complex(coeff)
+        _lib.check("dmrg_krylov_expm", self.lib.dmrg_krylov_expm(
+            ctypes.byref(h), x.data_ptr(), coeff.real, coeff.imag, k, KRYLOV_TOL, KRYLOV_ERRGOAL,
+            ctypes.byref(it), ptr, size, self.stream))
+        return it.value
+
+    def gemm(self, A2, B2):
+        """C = A2 @ B2 for 2-D contiguous device tensors."""
+        torch = _torch()
+        m, k = A2.shape
+        k2, n = B2.shape
+        assert k == k2
+        C = torch.empty((m, n), dtype=self.tdtype, device=self.device)
+        need = self.lib.dmrg_gemm_workspace_bytes(self.cdtype, self.prec, m, k, n)
+        ptr, size = self.ws.get(need)
+        _lib.check("dmrg_gemm", self.lib.dmrg_gemm(self.cdtype, self.prec, m, k, n, A2.data_ptr(), B2.data_ptr(),
+                                                   C.data_ptr(), ptr, size, self.stream))
+        return C
+
+    def merge(self, Ai, Aj):
+        cl, d1, cm = Ai.shape
+        _, d2, cr = Aj.shape
+        return self.gemm(Ai.reshape(cl * d1, cm), Aj.reshape(cm, d2 * cr)).reshape(cl, d1, d2, cr)
+
+    def svd(self, M2, cutoff, maxdim, mindim=1, absorb=0):
+        """Truncated SVD of a 2-D device matrix -> (left, right, s, keep, disc)."""
+        torch = _torch()
+        m, n = M2.shape
+        cap = min(m, n) if not maxdim or maxdim <= 0 else min(m, n, maxdim)
+        lo = torch.empty(m * cap, dtype=self.tdtype, device=self.device)
+        ro = torch.empty(cap * n, dtype=self.tdtype, device=self.device)
+        s = np.zeros(min(m, n), dtype=np.float64)
+        keep = ctypes.c_int(0)
+        disc = ctypes.c_double(0.0)
+        need = self.lib.dmrg_svd_workspace_bytes(self.cdtype, m, n)
+        ptr, size = self.ws.get(need)
+        st = self.lib.dmrg_svd_truncate(self.cdtype, m, n, M2.data_ptr(), float(cutoff),
+                                        int(maxdim) if maxdim else 0, int(mindim), int(absorb),
+                                        lo.data_ptr(), ro.data_ptr(),
+                                        s.ctypes.data_as(_lib.P_double), ctypes.byref(keep), ctypes.byref(disc),
+                                        ptr, size, self.stream)
+        _lib.check("dmrg_svd_truncate", st)
+        k = keep.value
+        return lo[:m * k].view(m, k), ro[:k * n].view(k, n), s, k, disc.value
+
+    def env_left(self, L, W, A):
+        torch = _torch()
+        cl, d, cr = A.shape
+        wl, wr = W.shape[0], W.shape[3]
+        out = torch.empty((cr, wr, cr), dtype=self.tdtype, device=self.device)
+        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, self.prec, cl, d, cr, wl, wr)
+        ptr, size = self.ws.get(need)
+        _lib.check("dmrg_env_extend_left", self.lib.dmrg_env_extend_left(
+            self.cdtype, self.prec, cl, d, cr, wl, wr, L.data_ptr(), W.data_ptr(), A.data_ptr(), out.data_ptr(),
+            ptr, size, self.stream))
+        return out
+
+    def env_right(self, R, W, B):
+        torch = _torch()
+        cl, d, cr = B.shape
+        wl, wr = W.shape[0], W.shape[3]
+        out = torch.empty((cl, wl, cl), dtype=self.tdtype, device=self.device)
+        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, self.prec, cl, d, cr, wl, wr)
+        ptr, size = self.ws.get(need)
+        _lib.check("dmrg_env_extend_right", self.lib.dmrg_env_extend_right(
+            self.cdtype, self.prec, cl, d, cr, wl, wr, R.data_ptr(), W.data_ptr(), B.data_ptr(), out.data_ptr(),
+            ptr, size, self.stream))
+        return out
+
+    def right_envs(self, A):
+        n = len(A)
+        env = {n + 1: self.edge}
+        for i in range(n, 1, -1):
+            env[i] = self.env_right(env[i + 1], self.W[i - 1], A[i - 1])
+        return env
+
+    def left_envs(self, A):
+        n = len(A)
+        env = {0: self.edge}
+        for i in range(1, n):
+            env[i] = self.env_left(env[i - 1], self.W[i - 1], A[i - 1])
+        return env
+
+    # ------------------------------------------------------------ DMRG
+    @staticmethod
+    def heff2_flops(cl, d1, d2, cr, wl, wm, wr, complex_=False):
+        """Algorithmic FLOPs of one two-site matvec (2 per real MAC; complex
+        MACs count 4 real MACs)."""
+        macs = cl * wl * cl * d1 * d2 * cr + cl * d1 * wm * wl * d1 * d2 * cr \
+            + cl * d1 * d2 * wr * wm * d2 * cr + cl * d1 * d2 * cr * wr * cr
+        return 2.0 * macs * (4 if complex_ else 1)
+
+    def _bond_update(self, L, Wi, Wj, R, Ai, Aj, niter, cutoff, maxdim, absorb, record):
+        torch = _torch()
+        t0 = time.perf_counter()
+        theta = self.merge(Ai, Aj).contiguous()
+        t1 = time.perf_counter()
+        h = self.heff2(L, Wi, Wj, R, theta.shape)
+        energy, k = self.ground(h, theta, niter)
+        t2 = time.perf_counter()
+        cl, d1, d2, cr = theta.shape
+        lo, ro, s, keep, disc = self.svd(theta.view(cl * d1, d2 * cr), cutoff, maxdim, 1, absorb)
+        t3 = time.perf_counter()
+        st = self.stats
+        st.t["merge"] += t1 - t0
+        st.t["lanczos"] += t2 - t1
+        st.t["svd"] += t3 - t2
+        st.matvecs += k
+        st.matvec_flops += k * self.heff2_flops(cl, d1, d2, cr, Wi.shape[0], Wi.shape[3], Wj.shape[3], not self.real)
+        if record:
+            st.add(energy=energy, iters=k, keep=keep, disc=disc, chil=cl, chir=cr)
+        return energy, lo.view(cl, d1, keep), ro.view(keep, d2, cr), s, keep, disc
+
+    def sweep(self, A, maxdim, cutoff, niter=2, record=False):
+        """One left-to-right then right-to-left two-site sweep on the list of
+        device site tensors A (modified in place); returns the last bond's
+        eigenvalue (pyitensor/dmrg.py:355-382)."""
+        n = len(A)
+        W = self.W
+        renv = self._renv if self._renv is not None else self.right_envs(A)
+        lenv = {0: self.edge}
+        energy = None
+        for i in range(1, n):
+            energy, A[i - 1], A[i], _, _, _ = self._bond_update(
+                lenv[i - 1], W[i - 1], W[i], renv[i + 2], A[i - 1], A[i], niter, cutoff, maxdim, 0, record)
+            t0 = time.perf_counter()
+            lenv[i] = self.env_left(lenv[i - 1], W[i - 1], A[i - 1])
+            self.stats.t["env"] += time.perf_counter() - t0
+        renv = {n + 1: self.edge}
+        for i in range(n - 1, 0, -1):
+            energy, A[i - 1], A[i], _, _, _ = self._bond_update(
+                lenv[i - 1], W[i - 1], W[i], renv[i + 2], A[i - 1], A[i], niter, cutoff, maxdim, 1, record)
+            t0 = time.perf_counter()
+            renv[i + 1] = self.env_right(renv[i + 2], W[i], A[i])
+            self.stats.t["env"] += time.perf_counter() - t0
+        # the right environments now match A exactly (every A[i], i >= 2, was
+        # finalised before its environment was built), so the next sweep
+        # reuses them instead of rebuilding (pyitensor/dmrg.py:365 rebuilds)
+        self._renv = renv
+        return energy
+
+    def dmrg(self, A, maxdims, cutoffs, niters=2, record=False):
+        """pyitensor/dmrg.py:385-398 with one (maxdim, cutoff, niter) per sweep."""
+        nsw = len(maxdims)
+        cutoffs = list(cutoffs) if isinstance(cutoffs, (list, tuple)) else [cutoffs] * nsw
+        niters = list(niters) if isinstance(niters, (list, tuple)) else [niters] * nsw
+        self._renv = None
+        energy = None
+        for s in range(nsw):
+            energy = self.sweep(A, maxdims[s], cutoffs[s], niters[s], record)
+        return energy
+
+    def invalidate(self):
+        self._renv = None
+
+    # ------------------------------------------------------------ initial state
+    def canonicalize_right_to_left_of(self, A):
+        """Lossless left-to-right SVD pass (centre ends at the last site) and
+        normalisation: pyitensor/mpsalgebra.py:347-352 (position(n), normalize)."""
+        n = len(A)
+        for i in range(n - 1):
+            cl, d, cr = A[i].shape
+            lo, ro, s, keep, _ = self.svd(A[i].reshape(cl * d, cr), 0.0, 0, 1, 0)
+            A[i] = lo.reshape(cl, d, keep)
+            A[i + 1] = self.gemm(ro, A[i + 1].reshape(cr, -1)).reshape(keep, A[i + 1].shape[1], A[i + 1].shape[2])
+        nrm = float(_torch().linalg.vector_norm(A[n - 1]).item())
+        A[n - 1] = A[n - 1] / nrm
+        return A
+
+    # ------------------------------------------------------------ TDVP
+    def _evolve2(self, L, Wi, Wj, R, theta, coeff, niter):
+        h = self.heff2(L, Wi, Wj, R, theta.shape)
+        self.expm(h, theta, coeff, niter)
+        return theta
+
+    def _evolve1(self, L, W, R, A, coeff, niter):
+        A = A.contiguous().clone()
+        h = self.heff1(L, W, R, A.shape)
+        self.expm(h, A, coeff, niter)
+        return A
+
+    def _evolve0(self, L, R, C, coeff, niter):
+        C = C.contiguous().clone()
+        h = self.heff0(L, R, C.shape)
+        self.expm(h, C, coeff, niter)
+        return C
+
+    def tdvp_step(self, A, dt, cutoff, maxdim, niter=50, num_center=2):
+        """One step exp(-i dt H): two half sweeps of dt/2 (pyitensor/tdvp.py:350-368)."""
+        if self.real:
+            raise ValueError("real-time TDVP needs a complex engine (real=False)")
+        tau = dt / 2.0
+        n = len(A)
+        W = self.W
+        self._renv = None
+        if num_center == 1:
+            renv = self.right_envs(A)
+            lenv = {0: self.edge}
+            for i in range(1, n + 1):
+                Anew = self._evolve1(lenv[i - 1], W[i - 1], renv[i + 1], A[i - 1], -1j * tau, niter)
+                if i == n:
+                    A[i - 1] = Anew
+                    continue
+                cl, d, cr = Anew.shape
+                Q, C, _, k, _ = self.svd(Anew.reshape(cl * d, cr), -1.0, 0, 1, 0)
+                A[i - 1] = Q.reshape(cl, d, k)
+                lenv[i] = self.env_left(lenv[i - 1], W[i - 1], A[i - 1])
+                Cev = self._evolve0(lenv[i], renv[i + 1], C, 1j * tau, niter)
+                nxt = A[i]
+                A[i] = self.gemm(Cev, nxt.reshape(cr, -1)).reshape(k, nxt.shape[1], nxt.shape[2])
+            lenv = self.left_envs(A)
+            renv = {n + 1: self.edge}
+            for i in range(n, 0, -1):
+                Anew = self._evolve1(lenv[i - 1], W[i - 1], renv[i + 1], A[i - 1], -1j * tau, niter)
+                if i == 1:
+                    A[0] = Anew
+                    continue
+                cl, d, cr = Anew.shape
+                C, V, _, k, _ = self.svd(Anew.reshape(cl, d * cr), -1.0, 0, 1, 1)
+                A[i - 1] = V.reshape(k, d, cr)
+                renv[i] = self.env_right(renv[i + 1], W[i - 1], A[i - 1])
+                Cev = self._evolve0(lenv[i - 1], renv[i], C, 1j * tau, niter)
+                prv = A[i - 2]
+                A[i - 2] = self.gemm(prv.reshape(-1, cl), Cev).reshape(prv.shape[0], prv.shape[1], k)
+            return A
+        # two-site
+        renv = self.right_envs(A)
+        lenv = {0: self.edge}
+        for i in range(1, n):
+            theta = self.merge(A[i - 1], A[i]).contiguous()
+            theta = self._evolve2(lenv[i - 1], W[i - 1], W[i], renv[i + 2], theta, -1j * tau, niter)
+            cl, d1, d2, cr = theta.shape
+            U, C, _, k, _ = self.svd(theta.view(cl * d1, d2 * cr), cutoff, maxdim, 1, 0)
+            A[i - 1] = U.reshape(cl, d1, k)
+            A[i] = C.reshape(k, d2, cr)
+            lenv[i] = self.env_left(lenv[i - 1], W[i - 1], A[i - 1])
+            if i < n - 1:
+                A[i] = self._evolve1(lenv[i], W[i], renv[i + 2], A[i], 1j * tau, niter)
+        lenv = self.left_envs(A)
+        renv = {n + 1: self.edge}
+        for i in range(n - 1, 0, -1):
+            theta = self.merge(A[i - 1], A[i]).contiguous()
+            theta = self._evolve2(lenv[i - 1], W[i - 1], W[i], renv[i + 2], theta, -1j * tau, niter)
+            cl, d1, d2, cr = theta.shape
+            C, V, _, k, _ = self.svd(theta.view(cl * d1, d2 * cr), cutoff, maxdim, 1, 1)
+            A[i] = V.reshape(k, d2, cr)
+            A[i - 1] = C.reshape(cl, d1, k)
+            renv[i + 1] = self.env_right(renv[i + 2], W[i], A[i])
+            if i > 1:
+                A[i - 1] = self._evolve1(lenv[i - 1], W[i - 1], renv[i + 1], A[i - 1], 1j * tau, niter)
+        return A

@@ -1,0 +1,154 @@
+/*
+ * dmrg_gb300.h -- C ABI of the GB300 two-site DMRG/TDVP sweep library.
+ *
+ * Every entry point takes plain device pointers, sizes and a cudaStream_t
+ * (passed as void*), allocates nothing itself (scratch comes from a
+ * caller-provided workspace whose size the matching *_workspace_bytes()
+ * reports), and returns an int status (DMRG_OK = 0).  No entry point
+ * traps, aborts or waits without a bound.
+ *
+ * Array layouts (row-major, element type double or interleaved complex
+ * double as selected by `dtype`):
+ *   MPS site tensor A      (chi_left, d, chi_right)
+ *   MPO site tensor W      (w_left, d_in, d_out, w_right)   d_in = ket leg
+ *   left environment L     (chi_bra, w, chi_ket)
+ *   right environment R    (chi_bra, w, chi_ket)
+ *   two-site centre theta  (chi_left, d1, d2, chi_right)
+ *
+ * The functions replace the numerical kernels of dmrgpy's pure-Python
+ * backend (src/dmrgpy/pyitensor); each declaration cites the reference
+ * function it stands in for.
+ */
+#ifndef DMRG_GB300_H
+#define DMRG_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define DMRG_OK              0
+#define DMRG_ERR_ARG         1  /* bad shape, null pointer or unsupported combination */
+#define DMRG_ERR_WORKSPACE   2  /* caller workspace smaller than *_workspace_bytes() */
+#define DMRG_ERR_CUDA        3  /* a CUDA runtime call or kernel launch failed */
+#define DMRG_ERR_NAN         4  /* a non-finite value reached a reduction */
+#define DMRG_ERR_NOCONV      5  /* an iterative eigensolver hit its sweep limit */
+#define DMRG_ERR_TIMEOUT     6  /* a bounded device-side wait gave up */
+#define DMRG_ERR_UNSUPPORTED 7  /* combination not built (e.g. complex + TF32x3) */
+
+/* ---- element types and contraction precisions ------------------------ */
+#define DMRG_REAL64      0
+#define DMRG_COMPLEX128  1
+#define DMRG_PREC_FP64   0  /* all contractions in FP64 */
+#define DMRG_PREC_TF32X3 1  /* bulk contractions as split-TF32 (3 products,
+                               FP32 accumulation) on tcgen05; vectors and
+                               reductions stay FP64 */
+
+/* Effective-Hamiltonian operator of one bond/site.
+ *   kind 2: y = L . W1 . W2 . R . theta  over theta (chil, d1, d2, chir)
+ *           (pyitensor/dmrg.py:224-248 two_site_heff, the plan of
+ *            pyitensor/kernels.py:298-410)
+ *   kind 1: y = L . W1 . R . A            over A (chil, d1, chir)
+ *           (pyitensor/dmrg.py:251-275 one_site_heff)
+ *   kind 0: y = L . R . C                 over C (chil, chir)
+ *           (pyitensor/dmrg.py:278-299 zero_site_heff)
+ * MPO bonds: W1 is (wl, d1, d1, wm), W2 is (wm, d2, d2, wr); for kind 1
+ * W1 is (wl, d1, d1, wr); for kind 0, wl == wr and W1/W2 are unused.
+ * L is (chil, wl, chil), R is (chir, wr, chir). */
+typedef struct dmrg_heff_t {
+  int kind;
+  int dtype;
+  int precision;
+  int chil, d1, d2, chir;
+  int wl, wm, wr;
+  const void* L;
+  const void* W1;
+  const void* W2;
+  const void* R;
+} dmrg_heff_t;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int dmrg_version(void);
+/* Static description of a status code. */
+const char* dmrg_status_string(int status);
+
+/* ---- effective-Hamiltonian matvec ------------------------------------- */
+/* Workspace for dmrg_heff_apply (also covers the operand preparation). */
+size_t dmrg_heff_workspace_bytes(const dmrg_heff_t* op);
+/* y = H_eff x.  Replaces the matvec closure of pyitensor/kernels.py:353-410
+ * (_make_matvec_planned) built by pyitensor/dmrg.py:224-299.  x and y must
+ * not alias. */
+int dmrg_heff_apply(const dmrg_heff_t* op, const void* x, void* y,
+                    void* work, size_t work_bytes, void* stream);
+
+/* ---- environments ----------------------------------------------------- */
+size_t dmrg_env_workspace_bytes(int dtype, int precision, int chil, int d, int chir, int wl, int wr);
+/* Lnew (chir, wr, chir) = L (chil, wl, chil) . conj(A) . W . A with
+ * A (chil, d, chir), W (wl, d, d, wr).  Replaces pyitensor/dmrg.py:170-191
+ * (_extend_left). */
+int dmrg_env_extend_left(int dtype, int precision, int chil, int d, int chir, int wl, int wr,
+                         const void* L, const void* W, const void* A, void* Lnew,
+                         void* work, size_t work_bytes, void* stream);
+/* Rnew (chil, wl, chil) = R (chir, wr, chir) . conj(B) . W . B with
+ * B (chil, d, chir).  Replaces pyitensor/dmrg.py:194-201 (_extend_right). */
+int dmrg_env_extend_right(int dtype, int precision, int chil, int d, int chir, int wl, int wr,
+                          const void* R, const void* W, const void* B, void* Rnew,
+                          void* work, size_t work_bytes, void* stream);
+
+/* ---- Krylov solvers ------------------------------------------------------ */
+size_t dmrg_lanczos_workspace_bytes(const dmrg_heff_t* op, int niter);
+/* Lowest eigenpair of H_eff by Lanczos with full reorthogonalisation; stops
+ * when the lowest Ritz value moves by less than tol*max(1,|E|), when the
+ * residual norm drops below tol, or after niter matvecs.  x holds the start
+ * vector on entry and the normalised eigenvector on exit.  Replaces
+ * pyitensor/dmrg.py:95-142 (_lanczos_ground_state) as driven by
+ * pyitensor/dmrg.py:302-333 (_local_ground_state). */
+int dmrg_lanczos_ground(const dmrg_heff_t* op, void* x, int niter, double tol,
+                        double* energy, int* iters,
+                        void* work, size_t work_bytes, void* stream);
+size_t dmrg_expm_workspace_bytes(const dmrg_heff_t* op, int niter);
+/* x <- exp(coeff * H_eff) x by a Krylov subspace of dimension <= niter with
+ * Saad's a-posteriori stop (beta0*beta_k*|e_k^T exp(coeff T) e_1| < errgoal).
+ * Complex dtype only.  Replaces pyitensor/tdvp.py:82-172
+ * (_lanczos_expm_multiply). */
+int dmrg_krylov_expm(const dmrg_heff_t* op, void* x, double coeff_re, double coeff_im,
+                     int niter, double tol, double errgoal, int* iters,
+                     void* work, size_t work_bytes, void* stream);
+
+/* ---- truncated factorisation --------------------------------------------- */
+size_t dmrg_svd_workspace_bytes(int dtype, int m, int n);
+/* Truncated SVD of the row-major m x n matrix M by one-sided (Hestenes)
+ * Jacobi in FP64 on the min(m,n) columns of M^H or M, followed by the
+ * cutoff/maxdim/mindim rule of pyitensor/svd.py:32-68.  The one-sided form
+ * keeps small singular values to high relative accuracy, so it covers both
+ * the Gram-matrix route of the reference and its exact-SVD fallback
+ * (pyitensor/svd.py:108-151).  Replaces pyitensor/svd.py:108-195
+ * (_svd_truncated, svd) as used by pyitensor/dmrg.py:336-352.
+ *   absorb = 0: left_out = U (m x keep), right_out = S.Vh (keep x n)
+ *   absorb = 1: left_out = U.S (m x keep), right_out = Vh (keep x n)
+ *   absorb = 2: left_out = U, right_out = Vh (S only in svals)
+ * maxdim <= 0 means no cap; cutoff < 0 keeps every value (lossless split).
+ * svals (host, min(m,n) doubles, descending), keep and discarded (host)
+ * receive the spectrum.  left_out/right_out must hold min(m,n,maxdim)
+ * columns/rows. */
+int dmrg_svd_truncate(int dtype, int m, int n, const void* M,
+                      double cutoff, int maxdim, int mindim, int absorb,
+                      void* left_out, void* right_out,
+                      double* svals, int* keep, double* discarded,
+                      void* work, size_t work_bytes, void* stream);
+
+/* ---- dense contraction ---------------------------------------------------- */
+size_t dmrg_gemm_workspace_bytes(int dtype, int precision, int m, int k, int n);
+/* C (m x n) = A (m x k) . B (k x n), all row-major.  Used for the two-site
+ * merge theta = A_i . A_{i+1} (pyitensor/dmrg.py:233, Ti * Tj) and for the
+ * bond-matrix absorption of one-site TDVP (pyitensor/tdvp.py:300-313). */
+int dmrg_gemm(int dtype, int precision, int m, int k, int n, const void* A, const void* B, void* C,
+              void* work, size_t work_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DMRG_GB300_H */
