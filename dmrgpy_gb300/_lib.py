@@ -44,8 +44,13 @@ class HeffDesc(ctypes.Structure):
 SIGNATURES = [
     ("dmrg_version", c_int, []),
     ("dmrg_status_string", ctypes.c_char_p, [c_int]),
+    ("dmrg_kernel_launches", ctypes.c_ulonglong, []),
     ("dmrg_heff_workspace_bytes", c_size_t, [ctypes.POINTER(HeffDesc)]),
     ("dmrg_heff_apply", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_heff_prepare", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_size_t, c_void_p]),
+    ("dmrg_heff_apply_prepared", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_void_p, c_void_p, c_size_t,
+                                         c_void_p]),
+    ("dmrg_heff_status", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_size_t, c_void_p]),
     ("dmrg_env_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     ("dmrg_env_extend_left", c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
@@ -60,6 +65,9 @@ SIGNATURES = [
     ("dmrg_svd_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
     ("dmrg_svd_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_double, c_int, c_int, c_int,
                                   c_void_p, c_void_p, P_double, P_int, P_double, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_subspace_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
+    ("dmrg_subspace_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
+                                       P_double, c_void_p, c_size_t, c_void_p]),
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),

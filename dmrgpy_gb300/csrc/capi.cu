@@ -10,7 +10,13 @@
 #include "heff.cuh"
 #include "tf32x3.cuh"
 
+#include <atomic>
+
 namespace dmrg {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 namespace {
 
 inline size_t esize(int dtype) { return dtype == DMRG_COMPLEX128 ? 16 : 8; }
@@ -43,11 +49,26 @@ size_t heff_ws(const dmrg_heff_t* o) {
   return align_up(P * esize(o->dtype)) + align_up(Q * esize(o->dtype));
 }
 
+// One-off preparation of an operator (split-TF32: operand splitting of L, R
+// and the two-site MPO), then heff_run per Krylov iteration.
+template <typename T>
+int heff_prepare(const dmrg_heff_t* o, void* work, cudaStream_t s) {
+  if (o->precision != DMRG_PREC_TF32X3) return DMRG_OK;
+  if (o->dtype != DMRG_REAL64) return DMRG_ERR_UNSUPPORTED;
+  return tf32x3_heff_prepare(*o, work, s);
+}
+
+template <typename T>
+int heff_finish(const dmrg_heff_t* o, void* work, cudaStream_t s) {
+  if (o->precision != DMRG_PREC_TF32X3) return DMRG_OK;
+  return tf32x3_heff_status(*o, work, s);
+}
+
 template <typename T>
 int heff_run(const dmrg_heff_t* o, const T* x, T* y, void* work, cudaStream_t s) {
   if (o->precision == DMRG_PREC_TF32X3) {
     if (o->dtype != DMRG_REAL64) return DMRG_ERR_UNSUPPORTED;
-    return tf32x3_heff_apply(*o, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), work, s);
+    return tf32x3_heff_apply_prepared(*o, reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y), work, s);
   }
   size_t P, Q;
   heff_fp64_elems<T>(*o, &P, &Q);
@@ -205,6 +226,7 @@ int lanczos_impl(const dmrg_heff_t* o, T* x, int niter, double tol, double* ener
     DMRG_TRY(vnorm<T>(x, n, nrm_d, ws.red, s));
   }
   DMRG_TRY(vscale_dev_inv<T>(Q, x, nrm_d, n, s));  // q0
+  DMRG_TRY(heff_prepare<T>(o, ws.hw, s));
   DMRG_TRY(heff_run<T>(o, Q, w, ws.hw, s));
   DMRG_TRY(vdot<T>(Q, w, n, reinterpret_cast<T*>(alpha_d), ws.red, s));
   DMRG_TRY(vaxpy2<T>(w, Q, alpha_d, nullptr, nullptr, n, s));
@@ -249,6 +271,7 @@ int lanczos_impl(const dmrg_heff_t* o, T* x, int niter, double tol, double* ener
   DMRG_CUDA_TRY(cudaMemcpyAsync(h, yt.data(), sizeof(T) * k, cudaMemcpyHostToDevice, s));
   DMRG_TRY(gemv_sub<T>(Q, n, k, h, x, n, 1, s));
   DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  DMRG_TRY(heff_finish<T>(o, ws.hw, s));
   if (energy) *energy = ev;
   if (iters) *iters = k;
   return DMRG_OK;
@@ -284,6 +307,7 @@ int expm_impl(const dmrg_heff_t* o, T* x, std::complex<double> coeff, int niter,
     return DMRG_OK;
   }
   DMRG_TRY(vscale_dev_inv<T>(Q, x, nrm_d, n, s));
+  DMRG_TRY(heff_prepare<T>(o, ws.hw, s));
   std::vector<double> al, be;
   for (int it = 0; it < m; ++it) {
     T* qi = Q + (long long)it * n;
@@ -320,6 +344,7 @@ int expm_impl(const dmrg_heff_t* o, T* x, std::complex<double> coeff, int niter,
       DMRG_CUDA_TRY(cudaMemcpyAsync(h, ct.data(), sizeof(T) * k, cudaMemcpyHostToDevice, s));
       DMRG_TRY(gemv_sub<T>(Q, n, k, h, x, n, 1, s));
       DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+      DMRG_TRY(heff_finish<T>(o, ws.hw, s));
       if (iters) *iters = k;
       return DMRG_OK;
     }
@@ -398,6 +423,8 @@ extern "C" {
 
 int dmrg_version(void) { return 100; }
 
+unsigned long long dmrg_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
 const char* dmrg_status_string(int status) {
   switch (status) {
     case DMRG_OK: return "ok";
@@ -422,7 +449,34 @@ int dmrg_heff_apply(const dmrg_heff_t* op, const void* x, void* y, void* work, s
   if (heff_ws(op) > work_bytes || (!work && heff_ws(op) > 0)) return DMRG_ERR_WORKSPACE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (op->dtype == DMRG_COMPLEX128) return heff_run<cplx>(op, static_cast<const cplx*>(x), static_cast<cplx*>(y), work, s);
+  DMRG_TRY(heff_prepare<double>(op, work, s));
+  DMRG_TRY(heff_run<double>(op, static_cast<const double*>(x), static_cast<double*>(y), work, s));
+  return heff_finish<double>(op, work, s);
+}
+
+int dmrg_heff_prepare(const dmrg_heff_t* op, void* work, size_t work_bytes, void* stream) {
+  if (!heff_valid(op)) return DMRG_ERR_ARG;
+  if (heff_ws(op) > work_bytes || (!work && heff_ws(op) > 0)) return DMRG_ERR_WORKSPACE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (op->dtype == DMRG_COMPLEX128) return heff_prepare<cplx>(op, work, s);
+  return heff_prepare<double>(op, work, s);
+}
+
+int dmrg_heff_apply_prepared(const dmrg_heff_t* op, const void* x, void* y, void* work, size_t work_bytes,
+                             void* stream) {
+  if (!heff_valid(op) || !x || !y || x == y) return DMRG_ERR_ARG;
+  if (heff_ws(op) > work_bytes || (!work && heff_ws(op) > 0)) return DMRG_ERR_WORKSPACE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (op->dtype == DMRG_COMPLEX128) return heff_run<cplx>(op, static_cast<const cplx*>(x), static_cast<cplx*>(y), work, s);
   return heff_run<double>(op, static_cast<const double*>(x), static_cast<double*>(y), work, s);
+}
+
+int dmrg_heff_status(const dmrg_heff_t* op, void* work, size_t work_bytes, void* stream) {
+  if (!heff_valid(op)) return DMRG_ERR_ARG;
+  if (heff_ws(op) > work_bytes) return DMRG_ERR_WORKSPACE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  return heff_finish<double>(op, work, s);
 }
 
 size_t dmrg_env_workspace_bytes(int dtype, int precision, int chil, int d, int chir, int wl, int wr) {
@@ -539,6 +593,21 @@ int dmrg_gemm(int dtype, int precision, int m, int k, int n, const void* A, cons
                        static_cast<cplx*>(C), s);
   return tgemm<double>(g, 1.0, static_cast<const double*>(A), static_cast<const double*>(B), 0.0,
                        static_cast<double*>(C), s);
+}
+
+size_t dmrg_subspace_workspace_bytes(int m, int n, int k) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  return subspace_workspace_bytes(m, n, k);
+}
+
+int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* start, int kstart, int absorb,
+                           void* left_out, void* right_out, double* discarded, void* work, size_t work_bytes,
+                           void* stream) {
+  if (m <= 0 || n <= 0 || k <= 0 || !theta || !left_out || !right_out || (kstart > 0 && !start)) return DMRG_ERR_ARG;
+  if (absorb != 0 && absorb != 1) return DMRG_ERR_ARG;
+  return subspace_truncate(m, n, k, static_cast<const double*>(theta), static_cast<const double*>(start), kstart,
+                           absorb, static_cast<double*>(left_out), static_cast<double*>(right_out), discarded, work,
+                           work_bytes, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -62,10 +62,14 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // ---------------------------------------------------------------- launch checks
+// Every kernel launch of the library is followed by this check, which also
+// counts the launch (dmrg_kernel_launches()).
+void count_launch();
 #define DMRG_CHECK_LAUNCH()                                      \
   do {                                                           \
     cudaError_t _e = cudaGetLastError();                         \
     if (_e != cudaSuccess) return DMRG_ERR_CUDA;                 \
+    ::dmrg::count_launch();                                      \
   } while (0)
 
 #define DMRG_CUDA_TRY(x)                                         \

@@ -64,9 +64,11 @@ struct HArgs {
   int r, c, cp;  // cp = c rounded up to even
   int max_sweeps;
   double tol;
+  const double* frob;  // |M|_F (device): absolute floor of the rotation test
   GridBar bar;
   unsigned* rotcnt;  // [3], used cyclically: sweep k counts into slot k%3
   int* sweeps_out;
+  int X_in_smem;
 };
 
 template <typename T>
@@ -114,6 +116,17 @@ __device__ __forceinline__ int player(int pos, int round, int cp) {
 
 template <typename T, bool COOP>
 __global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
+  extern __shared__ unsigned char hsm[];
+  // single-CTA variant: work on a shared-memory copy of X when it fits
+  T* const Xg = a.X;
+  if (!COOP && a.X_in_smem) {
+    T* xs = reinterpret_cast<T*>(hsm);
+    for (long long i = threadIdx.x; i < (long long)a.r * a.c; i += blockDim.x) xs[i] = Xg[i];
+    a.X = xs;
+    __syncthreads();
+  }
+  const double fro = *a.frob;
+  const double abs_floor = 1e-16 * fro * fro;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -150,7 +163,12 @@ __global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
         gim = warp_sum(gim);
         double ag = sqrt(gre * gre + gim * gim);
         double scale = sqrt(al * be);
-        if (!(ag > a.tol * scale) || !(ag > 1e-300)) continue;
+        // rotate only couplings above tol relative to the pair and above an
+        // absolute floor (1e-16 |M|_F^2): singular values come out to the
+        // absolute accuracy of a standard SVD without chasing the relative
+        // accuracy of negligible ones, which costs many extra sweeps on the
+        // steeply graded spectra of DMRG bonds
+        if (!(ag > a.tol * scale) || !(ag > abs_floor) || !(ag > 1e-300)) continue;
         double tau = (be - al) / (2.0 * ag);
         double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
         double cs = 1.0 / sqrt(1.0 + t * t);
@@ -165,6 +183,10 @@ __global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
     converged = (((volatile unsigned*)a.rotcnt)[sweep % 3] == 0u);
   }
   if (gtid == 0) *a.sweeps_out = converged ? sweep : -sweep;
+  if (!COOP && a.X_in_smem) {
+    __syncthreads();
+    for (long long i = threadIdx.x; i < (long long)a.r * a.c; i += blockDim.x) Xg[i] = a.X[i];
+  }
 }
 
 // sigma_j = |X_j|, one warp per column
@@ -270,14 +292,16 @@ struct SvdWork {
   double* sig;
   double* sorted;
   int* perm;
-  unsigned* ctrl;  // [0..1] barrier, [2..4] rotation counters, [5] err, [6] sweeps
+  unsigned* ctrl;  // [0..1] barrier, [2..4] rotation counters, [5] err, [6] sweeps, [8..9] |M|_F
+  double* red;     // reduction scratch
 };
 
 size_t svd_work_bytes(int dtype, int m, int n) {
   size_t es = dtype == DMRG_COMPLEX128 ? 16 : 8;
   size_t c = (size_t)(m < n ? m : n);
   size_t r = (size_t)(m < n ? n : m);
-  return align_up(r * c * es) + align_up(c * c * es) + 2 * align_up(c * 8) + align_up(c * 4) + align_up(64);
+  return align_up(r * c * es) + align_up(c * c * es) + 2 * align_up(c * 8) + align_up(c * 4) + align_up(64) +
+         align_up((8 + 2 * 2 * 152) * 8);
 }
 
 static SvdWork carve(void* work, int dtype, int m, int n) {
@@ -291,7 +315,8 @@ static SvdWork carve(void* work, int dtype, int m, int n) {
   w.sig = reinterpret_cast<double*>(p); p += align_up(c * 8);
   w.sorted = reinterpret_cast<double*>(p); p += align_up(c * 8);
   w.perm = reinterpret_cast<int*>(p); p += align_up(c * 4);
-  w.ctrl = reinterpret_cast<unsigned*>(p);
+  w.ctrl = reinterpret_cast<unsigned*>(p); p += align_up(64);
+  w.red = reinterpret_cast<double*>(p);
   return w;
 }
 
@@ -307,6 +332,9 @@ int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* s
   DMRG_CUDA_TRY(cudaMemsetAsync(w.ctrl, 0, 64, s));
   load_x_kernel<T><<<egrid((long long)m * n), 256, 0, s>>>(M, m, n, left, static_cast<T*>(w.X));
   DMRG_CHECK_LAUNCH();
+  double* frob = reinterpret_cast<double*>(w.ctrl + 8);
+  DMRG_CUDA_TRY(cudaMemsetAsync(w.red, 0, 64, s));
+  DMRG_TRY(vnorm<T>(static_cast<const T*>(w.X), (long long)m * n, frob, w.red, s));
   HArgs<T> a;
   a.X = static_cast<T*>(w.X);
   a.V = static_cast<T*>(w.V);
@@ -321,12 +349,26 @@ int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* s
   a.rotcnt = w.ctrl + 2;
   a.bar.err = reinterpret_cast<int*>(w.ctrl + 5);
   a.sweeps_out = reinterpret_cast<int*>(w.ctrl + 6);
+  a.frob = frob;
+  a.X_in_smem = 0;
   const int half = a.cp / 2;
   // one CTA while the pairs of a round fit in 32 warps of one CTA and the
   // columns are short; otherwise a cooperative grid with one warp per pair
   if ((half <= 64 && (long long)r * c <= (1ll << 20)) || half <= 8) {
     int threads = 32 * (half < 32 ? (half > 0 ? half : 1) : 32);
-    hestenes_kernel<T, false><<<1, threads, 0, s>>>(a);
+    const size_t xbytes = sizeof(T) * (size_t)r * c;
+    size_t smem = 0;
+    if (xbytes <= 160 * 1024) {
+      a.X_in_smem = 1;
+      smem = xbytes;
+      static bool attr = false;
+      if (!attr) {
+        DMRG_CUDA_TRY(cudaFuncSetAttribute(hestenes_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+        DMRG_CUDA_TRY(cudaFuncSetAttribute(hestenes_kernel<cplx, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+        attr = true;
+      }
+    }
+    hestenes_kernel<T, false><<<1, threads, smem, s>>>(a);
     DMRG_CHECK_LAUNCH();
   } else {
     int dev = 0;
@@ -343,6 +385,7 @@ int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* s
     if (blocks < 1) blocks = 1;
     void* args[] = {&a};
     DMRG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)hestenes_kernel<T, true>, blocks, threads, args, 0, s));
+    count_launch();
   }
   colnorm_kernel<T><<<(c * 32 + 255) / 256, 256, 0, s>>>(a.X, r, c, w.sig);
   DMRG_CHECK_LAUNCH();

@@ -1,15 +1,848 @@
+// Split-TF32 contraction path on the 5th-generation tensor cores (sm_103a).
+//
+// Every FP64 operand x is split into two TF32 values, hi = tf32(x) and
+// lo = tf32(x - hi); a product is formed from three TF32 MMAs,
+// A_hi.B_hi + A_hi.B_lo + A_lo.B_hi, accumulated in FP32 in TMEM (the
+// lo.lo term is below FP32 resolution and dropped).  That gives FP32-level
+// accuracy (~1e-7 relative) at tensor-core rate.
+//
+// GEMM kernel (C[M,N] = sum_k A[M,k] B[N,k], both operands K-major):
+//   warp 0   TMA producer: per K-slice of 32 fp32 (one 128-byte swizzle
+//            row) loads the A_hi, A_lo, B_hi, B_lo tiles into a shared
+//            memory stage (SWIZZLE_128B), signalling an mbarrier with the
+//            transaction byte count;
+//   warp 1   allocates TMEM, then one elected thread issues
+//            tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=BN, K=8), four
+//            K-steps x three products per stage, and tcgen05.commit's the
+//            stage back to the producer;
+//   warps 2-5 epilogue: wait for the final commit, tcgen05.ld the 128 x BN
+//            FP32 accumulator (each warp reads its 32-lane TMEM quarter) and
+//            store FP32 or FP64 with arbitrary output strides.
+// All mbarrier waits are bounded (DMRG_ERR_TIMEOUT is recorded on expiry).
+//
+// Around the GEMMs: split kernels that produce the K-padded hi/lo operand
+// arrays (optionally transposing), and the MPO-step kernel that contracts
+// the two site MPO tensors into the GEMM1 output in one pass.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "tf32x3.cuh"
 
 namespace dmrg {
 
-size_t tf32x3_heff_workspace_bytes(const dmrg_heff_t&) { return 0; }
-int tf32x3_heff_apply(const dmrg_heff_t&, const double*, double*, void*, cudaStream_t) { return DMRG_ERR_UNSUPPORTED; }
-size_t tf32x3_env_workspace_bytes(int, int, int, int, int) { return 0; }
-int tf32x3_env(int, int, int, int, int, int, const double*, const double*, const double*, double*, void*, cudaStream_t) {
-  return DMRG_ERR_UNSUPPORTED;
+namespace {
+
+constexpr int BM = 128;     // accumulator rows = TMEM lanes
+constexpr int BN = 128;     // accumulator columns (fp32) per TMEM buffer
+constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
+constexpr int STAGES = 3;
+constexpr int NACC = 2;     // TMEM accumulator buffers (one K-slice each)
+constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
+constexpr int TILE_B_BYTES = BN * BK * 4;   // 16 KB
+constexpr int STAGE_BYTES = 2 * TILE_A_BYTES + 2 * TILE_B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align slack*/ + 256 /*barriers*/;
+constexpr int GEMM_THREADS = 192;           // 6 warps
+constexpr long long WAIT_CYCLES = 4000000000ll;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-size_t tf32x3_gemm_workspace_bytes(int, int, int) { return 0; }
-int tf32x3_gemm(int, int, int, const double*, const double*, double*, void*, cudaStream_t) { return DMRG_ERR_UNSUPPORTED; }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase; records a timeout and returns false if
+// the phase does not complete within WAIT_CYCLES.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > WAIT_CYCLES) {
+      atomicExch(err, DMRG_ERR_TIMEOUT);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// core groups 1024 bytes apart (SBO), descriptor version 1 (sm_100 family).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+  d |= static_cast<uint64_t>(1) << 16;              // LBO (unused for swizzled K-major)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;      // SBO
+  d |= static_cast<uint64_t>(1) << 46;              // version
+  d |= static_cast<uint64_t>(2) << 61;              // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor of kind::tf32: D fp32, A/B tf32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct GemmOut {
+  void* C;
+  long long ldm, ldn;   // element strides of C
+  int M, N;
+  int out_f64;          // 1: store double, 0: store float
+  int accumulate;       // 1: C += alpha*result, 0: C = alpha*result
+  float alpha;
+};
+
+// The tensor-core FP32 accumulation is not round-to-nearest: summed over a
+// long K its error grows linearly.  Each K-slice of 32 is therefore
+// accumulated into its own TMEM buffer (two buffers, double-buffered) and
+// the slice results are summed by the epilogue warps in FP32 registers with
+// ordinary rounding, so the biased part spans at most 32 products.
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
+    tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+                       const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
+                       GemmOut out, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_full = empty + STAGES;
+  uint64_t* acc_empty = acc_full + NACC;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + NACC);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const int n0 = blockIdx.y * BN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < NACC; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(NACC * BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      for (int kt = 0; kt < KT; ++kt) {
+        const int s = kt % STAGES;
+        const int it = kt / STAGES;
+        if (kt >= STAGES && !mbar_wait(&empty[s], (it - 1) & 1, err)) break;
+        unsigned char* st = smem + s * STAGE_BYTES;
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        const int x = kt * BK;
+        tma_load_2d(st, &mAhi, &full[s], x, m0);
+        tma_load_2d(st + TILE_A_BYTES, &mAlo, &full[s], x, m0);
+        tma_load_2d(st + 2 * TILE_A_BYTES, &mBhi, &full[s], x, n0);
+        tma_load_2d(st + 2 * TILE_A_BYTES + TILE_B_BYTES, &mBlo, &full[s], x, n0);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      for (int kt = 0; kt < KT; ++kt) {
+        const int s = kt % STAGES;
+        const int it = kt / STAGES;
+        const int b = kt % NACC;
+        const int u = kt / NACC;
+        if (!mbar_wait(&full[s], it & 1, err)) break;
+        if (kt >= NACC && !mbar_wait(&acc_empty[b], (u - 1) & 1, err)) break;
+        tc_fence_after();
+        const uint32_t d = tmem + b * BN;
+        const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+        const uint32_t ahi = base, alo = base + TILE_A_BYTES;
+        const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TILE_B_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < BK / 8; ++kk) {
+          const uint32_t o = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
+          const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
+          const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
+          mma_tf32(d, dah, dbh, idesc, kk != 0);
+          mma_tf32(d, dah, dbl, idesc, 1u);
+          mma_tf32(d, dal, dbh, idesc, 1u);
+        }
+        mma_commit(&empty[s]);
+        mma_commit(&acc_full[b]);
+      }
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4); one row per thread
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    float acc[BN];
+#pragma unroll
+    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+    bool ok = true;
+    for (int kt = 0; kt < KT && ok; ++kt) {
+      const int b = kt % NACC;
+      const int u = kt / NACC;
+      ok = mbar_wait(&acc_full[b], u & 1, err);
+      tc_fence_after();
+      if (ok) {
+#pragma unroll
+        for (int c = 0; c < BN; c += 16) {
+          float v[16];
+          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BN + c, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[c + j] += v[j];
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
+    }
+    const int gm = m0 + row;
+    if (ok && gm < out.M) {
+#pragma unroll
+      for (int c = 0; c < BN; ++c) {
+        const int gn = n0 + c;
+        if (gn < out.N) {
+          const long long o = (long long)gm * out.ldm + (long long)gn * out.ldn;
+          const float r = out.alpha * acc[c];
+          if (out.out_f64) {
+            double* C = static_cast<double*>(out.C);
+            C[o] = out.accumulate ? C[o] + (double)r : (double)r;
+          } else {
+            float* C = static_cast<float*>(out.C);
+            C[o] = out.accumulate ? C[o] + r : r;
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BN));
+  }
+}
+
+// ---------------------------------------------------------------- splitting
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void split2(double x, float& hi, float& lo) {
+  hi = to_tf32(static_cast<float>(x));
+  lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
+}
+
+// out[r][k] (r < R, k < Kp) = split(in[r*ldr + k*ldk]) for k < K, 0 beyond.
+template <typename Tin>
+__global__ void split_kernel(const Tin* __restrict__ in, long long ldr, long long ldk, int R, int K, int Kp,
+                             float* __restrict__ hi, float* __restrict__ lo) {
+  const long long total = (long long)R * Kp;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+    const int r = (int)(i / Kp);
+    const int k = (int)(i - (long long)r * Kp);
+    float h = 0.f, l = 0.f;
+    if (k < K) split2(static_cast<double>(in[(long long)r * ldr + (long long)k * ldk]), h, l);
+    hi[i] = h;
+    lo[i] = l;
+  }
+}
+
+// Transposing split through a 32x33 shared tile:
+// out[c][r] (c < C, r < Rp) = split(in[r*ld + c]) for r < R, 0 beyond.
+__global__ void split_transpose_kernel(const double* __restrict__ in, long long ld, int R, int C, int Rp,
+                                       float* __restrict__ hi, float* __restrict__ lo) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    const int r = r0 + j, c = c0 + tx;
+    t[j][tx] = (r < R && c < C) ? in[(long long)r * ld + c] : 0.0;
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int c = c0 + j, r = r0 + tx;
+    if (c < C && r < Rp) {
+      float h, l;
+      split2(t[tx][j], h, l);
+      hi[(long long)c * Rp + r] = h;
+      lo[(long long)c * Rp + r] = l;
+    }
+  }
+}
+
+// Combined two-site MPO W2[(s',t',n)][(s,t,k)] = sum_m Wi[k,s,s',m] Wj[m,t,t',n]
+__global__ void w2_kernel(const double* __restrict__ Wi, const double* __restrict__ Wj, int d1, int d2, int wl, int wm,
+                          int wr, float* __restrict__ W2) {
+  const int rows = d1 * d2 * wr, cols = d1 * d2 * wl;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows * cols; i += gridDim.x * blockDim.x) {
+    const int r = i / cols, c = i - r * cols;
+    const int sp = r / (d2 * wr), tp = (r / wr) % d2, n = r % wr;
+    const int s = c / (d2 * wl), t = (c / wl) % d2, k = c % wl;
+    double acc = 0.0;
+    for (int m = 0; m < wm; ++m)
+      acc += Wi[((k * d1 + s) * d1 + sp) * wm + m] * Wj[((m * d2 + t) * d2 + tp) * wr + n];
+    W2[i] = static_cast<float>(acc);
+  }
+}
+
+// MPO step of the two-site matvec:
+//   X3[(a',s',t')][n*chir + b] = sum_{s,t,k} W2[(s',t',n)][(s,t,k)] X1[(s,t,b)][(a',k)]
+// written as split TF32 (hi, lo) rows of padded length Kp.  A CTA takes 32
+// consecutive b and AT consecutive a'; a warp's lanes walk b so the stores
+// of a row are 128-byte coalesced.
+constexpr int MID_AT = 4;
+__global__ void __launch_bounds__(256) mpo_step_kernel(const float* __restrict__ X1, const float* __restrict__ W2,
+                                                       int chil, int d1, int d2, int chir, int wl, int wr, int Kp,
+                                                       float* __restrict__ hi, float* __restrict__ lo) {
+  extern __shared__ float sm[];
+  const int nst = d1 * d2;
+  const int in_cols = nst * wl;   // (s,t,k)
+  const int out_rows = nst * wr;  // (s',t',n)
+  float* sW = sm;                              // out_rows x in_cols
+  float* sX = sW + out_rows * in_cols;         // [a_local][(s,t,k)][b_local 32]
+  const int b0 = blockIdx.x * 32;
+  const int a0 = blockIdx.y * MID_AT;
+  const long long ldx = (long long)chil * wl;
+  for (int i = threadIdx.x; i < out_rows * in_cols; i += blockDim.x) sW[i] = W2[i];
+  // load X1 rows (s,t,b) for the b tile, columns (a',k) for the a' tile
+  const int ncolx = MID_AT * wl;
+  for (int i = threadIdx.x; i < nst * 32 * ncolx; i += blockDim.x) {
+    const int col = i % ncolx;
+    const int bl = (i / ncolx) % 32;
+    const int st = i / (ncolx * 32);
+    const int al = col / wl, k = col % wl;
+    const int b = b0 + bl, a = a0 + al;
+    float v = 0.f;
+    if (b < chir && a < chil) v = X1[((long long)st * chir + b) * ldx + (long long)a * wl + k];
+    sX[(al * in_cols + st * wl + k) * 32 + bl] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int b = b0 + lane;
+  for (int row = warp; row < MID_AT * out_rows; row += 8) {
+    const int al = row / out_rows, r = row % out_rows;
+    const int a = a0 + al;
+    if (a >= chil) continue;
+    const float* w = sW + r * in_cols;
+    const float* x = sX + (al * in_cols) * 32 + lane;
+    float acc = 0.f;
+    for (int c = 0; c < in_cols; ++c) acc = fmaf(w[c], x[c * 32], acc);
+    if (b < chir) {
+      const int sp_tp = r / wr, n = r % wr;
+      const long long o = ((long long)a * nst + sp_tp) * Kp + (long long)n * chir + b;
+      float h = to_tf32(acc);
+      hi[o] = h;
+      lo[o] = to_tf32(acc - h);
+    }
+  }
+}
+
+inline int egrid(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+inline int pad32(long long x) { return (int)((x + 31) / 32 * 32); }
+
+// ---------------------------------------------------------------- host side
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+int get_encoder() {
+  if (g_encode) return DMRG_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || fn == nullptr)
+    return DMRG_ERR_CUDA;
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return DMRG_OK;
+}
+
+// 2D fp32 row-major [rows][Kp] operand, box = (BK, box_rows), SWIZZLE_128B
+int make_map(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (Kp % BK) != 0) return DMRG_ERR_ARG;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? DMRG_OK : DMRG_ERR_ARG;
+}
+
+bool g_attr_set = false;
+
+// C (M x N) = A (M x Kp) . B (N x Kp)^T from split operands.
+int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
+               const GemmOut& out, int* err, cudaStream_t s) {
+  DMRG_TRY(get_encoder());
+  CUtensorMap mah, mal, mbh, mbl;
+  DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM));
+  DMRG_TRY(make_map(&mal, Alo, M, Kp, BM));
+  DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BN));
+  DMRG_TRY(make_map(&mbl, Blo, N, Kp, BN));
+  if (!g_attr_set) {
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    g_attr_set = true;
+  }
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  if (grid.y > 65535) return DMRG_ERR_ARG;
+  tf32x3_gemm_kernel<<<grid, GEMM_THREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, Kp / BK, out, err);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+int split_rows(const double* in, long long ldr, long long ldk, int R, int K, int Kp, float* hi, float* lo,
+               cudaStream_t s) {
+  split_kernel<double><<<egrid((long long)R * Kp), 256, 0, s>>>(in, ldr, ldk, R, K, Kp, hi, lo);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+int split_transpose(const double* in, long long ld, int R, int C, int Rp, float* hi, float* lo, cudaStream_t s) {
+  dim3 grid((C + 31) / 32, (Rp + 31) / 32);
+  if (grid.y > 65535) return DMRG_ERR_ARG;
+  split_transpose_kernel<<<grid, 256, 0, s>>>(in, ld, R, C, Rp, hi, lo);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+// ---------------------------------------------------------------- two-site matvec plan
+struct Heff2Plan {
+  int cl, d1, d2, cr, wl, wm, wr;
+  int Kp1, Kp4;
+  long long M1, N1, M4;
+  float *thT_hi, *thT_lo, *L_hi, *L_lo, *X1, *X3_hi, *X3_lo, *R_hi, *R_lo, *W2;
+  int* err;
+  size_t bytes;
+};
+
+Heff2Plan plan2(const dmrg_heff_t& o, void* work) {
+  Heff2Plan p;
+  p.cl = o.chil; p.d1 = o.d1; p.d2 = o.d2; p.cr = o.chir; p.wl = o.wl; p.wm = o.wm; p.wr = o.wr;
+  p.Kp1 = pad32(p.cl);
+  p.Kp4 = pad32((long long)p.wr * p.cr);
+  p.M1 = (long long)p.d1 * p.d2 * p.cr;
+  p.N1 = (long long)p.cl * p.wl;
+  p.M4 = (long long)p.cl * p.d1 * p.d2;
+  char* b = static_cast<char*>(work);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    void* q = b ? b + off : nullptr;
+    off += align_up(bytes, 1024);
+    return q;
+  };
+  p.err = static_cast<int*>(take(256));
+  p.W2 = static_cast<float*>(take(sizeof(float) * (size_t)p.d1 * p.d2 * p.wr * p.d1 * p.d2 * p.wl));
+  p.L_hi = static_cast<float*>(take(sizeof(float) * p.N1 * p.Kp1));
+  p.L_lo = static_cast<float*>(take(sizeof(float) * p.N1 * p.Kp1));
+  p.R_hi = static_cast<float*>(take(sizeof(float) * (size_t)p.cr * p.Kp4));
+  p.R_lo = static_cast<float*>(take(sizeof(float) * (size_t)p.cr * p.Kp4));
+  p.thT_hi = static_cast<float*>(take(sizeof(float) * p.M1 * p.Kp1));
+  p.thT_lo = static_cast<float*>(take(sizeof(float) * p.M1 * p.Kp1));
+  p.X1 = static_cast<float*>(take(sizeof(float) * p.M1 * p.N1));
+  p.X3_hi = static_cast<float*>(take(sizeof(float) * p.M4 * p.Kp4));
+  p.X3_lo = static_cast<float*>(take(sizeof(float) * p.M4 * p.Kp4));
+  p.bytes = off;
+  return p;
+}
+
+}  // namespace
+
+size_t tf32x3_heff_workspace_bytes(const dmrg_heff_t& o) {
+  if (o.kind != 2) return 0;
+  return plan2(o, nullptr).bytes;
+}
+
+int tf32x3_heff_prepare(const dmrg_heff_t& o, void* work, cudaStream_t s) {
+  if (o.kind != 2 || o.dtype != DMRG_REAL64) return DMRG_ERR_UNSUPPORTED;
+  Heff2Plan p = plan2(o, work);
+  DMRG_CUDA_TRY(cudaMemsetAsync(p.err, 0, 256, s));
+  const int w2n = p.d1 * p.d2 * p.wr * p.d1 * p.d2 * p.wl;
+  w2_kernel<<<(w2n + 255) / 256, 256, 0, s>>>(static_cast<const double*>(o.W1), static_cast<const double*>(o.W2),
+                                              p.d1, p.d2, p.wl, p.wm, p.wr, p.W2);
+  DMRG_CHECK_LAUNCH();
+  // L (cl, wl, cl) as rows (a',k), K = a
+  DMRG_TRY(split_rows(static_cast<const double*>(o.L), p.cl, 1, (int)p.N1, p.cl, p.Kp1, p.L_hi, p.L_lo, s));
+  // R (cr, wr, cr) as rows b', K = (n, b)
+  DMRG_TRY(split_rows(static_cast<const double*>(o.R), (long long)p.wr * p.cr, 1, p.cr, p.wr * p.cr, p.Kp4, p.R_hi,
+                      p.R_lo, s));
+  // padding columns of X3 stay zero for every later matvec
+  DMRG_CUDA_TRY(cudaMemsetAsync(p.X3_hi, 0, sizeof(float) * p.M4 * p.Kp4, s));
+  DMRG_CUDA_TRY(cudaMemsetAsync(p.X3_lo, 0, sizeof(float) * p.M4 * p.Kp4, s));
+  return DMRG_OK;
+}
+
+int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s) {
+  Heff2Plan p = plan2(o, work);
+  // theta (cl, d1 d2 cr) -> thetaT rows (s,t,b), K = a
+  DMRG_TRY(split_transpose(x, p.M1, p.cl, (int)p.M1, p.Kp1, p.thT_hi, p.thT_lo, s));
+  GemmOut g1{p.X1, p.N1, 1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
+  DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
+  const int nst = p.d1 * p.d2;
+  const size_t smem = sizeof(float) * ((size_t)nst * p.wr * nst * p.wl + (size_t)MID_AT * nst * p.wl * 32);
+  if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
+  static bool attr = false;
+  if (!attr) {
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  dim3 grid((p.cr + 31) / 32, (p.cl + MID_AT - 1) / MID_AT);
+  if (grid.y > 65535) return DMRG_ERR_ARG;
+  mpo_step_kernel<<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi, p.X3_lo);
+  DMRG_CHECK_LAUNCH();
+  GemmOut g4{y, p.cr, 1, (int)p.M4, p.cr, 1, 0, 1.f};
+  DMRG_TRY(gemm_split(p.X3_hi, p.X3_lo, p.R_hi, p.R_lo, (int)p.M4, p.cr, p.Kp4, g4, p.err, s));
+  return DMRG_OK;
+}
+
+int tf32x3_heff_status(const dmrg_heff_t& o, void* work, cudaStream_t s) {
+  Heff2Plan p = plan2(o, work);
+  int h = 0;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(&h, p.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
+
+int tf32x3_heff_apply(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s) {
+  DMRG_TRY(tf32x3_heff_prepare(o, work, s));
+  DMRG_TRY(tf32x3_heff_apply_prepared(o, x, y, work, s));
+  return tf32x3_heff_status(o, work, s);
+}
+
+// ---------------------------------------------------------------- general GEMM
+// C (m x n, ldc) (+)= alpha * op(A) op(B); op(A) is m x k, op(B) is k x n.
+// A stored row-major with leading dim lda: transA=0 -> A[i*lda + kk],
+// transA=1 -> A[kk*lda + i].  B likewise: transB=0 -> B[kk*ldb + j],
+// transB=1 -> B[j*ldb + kk].
+size_t tf32x3_gemm_ex_workspace_bytes(int m, int n, int k) {
+  const size_t Kp = pad32(k);
+  return align_up(256, 1024) + 2 * align_up(sizeof(float) * (size_t)m * Kp, 1024) +
+         2 * align_up(sizeof(float) * (size_t)n * Kp, 1024);
+}
+
+int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, const double* A, long long lda,
+                   const double* B, long long ldb, int accumulate, double* C, long long ldc, void* work, int* err,
+                   cudaStream_t s) {
+  const int Kp = pad32(k);
+  char* b = static_cast<char*>(work) + align_up(256, 1024);
+  float* ahi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)m * Kp, 1024);
+  float* alo = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)m * Kp, 1024);
+  float* bhi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)n * Kp, 1024);
+  float* blo = reinterpret_cast<float*>(b);
+  if (!transA) DMRG_TRY(split_rows(A, lda, 1, m, k, Kp, ahi, alo, s));
+  else DMRG_TRY(split_transpose(A, lda, k, m, Kp, ahi, alo, s));
+  if (transB) DMRG_TRY(split_rows(B, ldb, 1, n, k, Kp, bhi, blo, s));
+  else DMRG_TRY(split_transpose(B, ldb, k, n, Kp, bhi, blo, s));
+  GemmOut g{C, ldc, 1, m, n, 1, accumulate, alpha};
+  return gemm_split(ahi, alo, bhi, blo, m, n, Kp, g, err, s);
+}
+
+// ---------------------------------------------------------------- plain GEMM (merges)
+size_t tf32x3_gemm_workspace_bytes(int m, int k, int n) {
+  const size_t Kp = pad32(k);
+  return align_up(256, 1024) + 2 * align_up(sizeof(float) * (size_t)m * Kp, 1024) +
+         2 * align_up(sizeof(float) * (size_t)n * Kp, 1024);
+}
+
+int tf32x3_gemm(int m, int k, int n, const double* A, const double* B, double* C, void* work, cudaStream_t s) {
+  const int Kp = pad32(k);
+  char* b = static_cast<char*>(work);
+  int* err = reinterpret_cast<int*>(b);
+  b += align_up(256, 1024);
+  float* ahi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)m * Kp, 1024);
+  float* alo = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)m * Kp, 1024);
+  float* bhi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)n * Kp, 1024);
+  float* blo = reinterpret_cast<float*>(b);
+  DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  DMRG_TRY(split_rows(A, k, 1, m, k, Kp, ahi, alo, s));
+  DMRG_TRY(split_transpose(B, n, k, n, Kp, bhi, blo, s));
+  GemmOut g{C, n, 1, m, n, 1, 0, 1.f};
+  DMRG_TRY(gemm_split(ahi, alo, bhi, blo, m, n, Kp, g, err, s));
+  int h = 0;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
+
+// ---------------------------------------------------------------- environments
+// Left:  Y1[(s,b)][(a',k)]  = sum_a   A^T[(s,b)][a] L[(a',k)][a]            (GEMM)
+//        Y2[(m,b)][(a',s')] = sum_{k,s} W[k,s,s',m] Y1[(s,b)][(a',k)]        (MPO step)
+//        Lnew[b'][(m,b)]    = sum_{(a',s')} A^T[b'][(a',s')] Y2[(m,b)][(a',s')]  (GEMM)
+// Right: Z1[(a,s)][(b',m)]  = sum_b   B[(a,s)][b] R[(b',m)][b]              (GEMM)
+//        Z2[(k,a)][(s',b')] = sum_{s,m} W[k,s,s',m] Z1[(a,s)][(b',m)]        (MPO step)
+//        Rnew[a'][(k,a)]    = sum_{(s',b')} B[a'][(s',b')] Z2[(k,a)][(s',b')]    (GEMM)
+namespace {
+
+// Y2 (left): CTA = 32 consecutive a' (lanes) x EB consecutive b.
+constexpr int EB = 8;
+__global__ void __launch_bounds__(256) env_left_mpo_kernel(const float* __restrict__ Y1, const double* __restrict__ W,
+                                                           int chil, int d, int chir, int wl, int wr, int Kp,
+                                                           float* __restrict__ hi, float* __restrict__ lo) {
+  extern __shared__ float sm[];
+  const int nin = d * wl, nout = d * wr;
+  float* sW = sm;                    // [(s',m)][(s,k)]
+  float* sX = sW + nout * nin;       // [b_local][(s,k)][a_local 32]
+  const int a0 = blockIdx.x * 32, b0 = blockIdx.y * EB;
+  for (int i = threadIdx.x; i < nout * nin; i += blockDim.x) {
+    const int r = i / nin, c = i % nin;
+    const int sp = r / wr, m = r % wr, s = c / wl, k = c % wl;
+    sW[i] = static_cast<float>(W[((k * d + s) * d + sp) * wr + m]);
+  }
+  const long long ldy = (long long)chil * wl;
+  for (int i = threadIdx.x; i < EB * d * 32 * wl; i += blockDim.x) {
+    const int col = i % (32 * wl);            // (a_local, k) contiguous in Y1
+    const int s = (i / (32 * wl)) % d;
+    const int bl = i / (32 * wl * d);
+    const int al = col / wl, k = col % wl;
+    const int a = a0 + al, b = b0 + bl;
+    float v = 0.f;
+    if (a < chil && b < chir) v = Y1[((long long)s * chir + b) * ldy + (long long)a * wl + k];
+    sX[(bl * nin + s * wl + k) * 32 + al] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int a = a0 + lane;
+  for (int row = warp; row < EB * nout; row += 8) {
+    const int bl = row / nout, r = row % nout;
+    const int b = b0 + bl;
+    if (b >= chir) continue;
+    const float* w = sW + r * nin;
+    const float* x = sX + (bl * nin) * 32 + lane;
+    float acc = 0.f;
+    for (int c = 0; c < nin; ++c) acc = fmaf(w[c], x[c * 32], acc);
+    if (a < chil) {
+      const int sp = r / wr, m = r % wr;
+      const long long o = ((long long)m * chir + b) * Kp + (long long)a * d + sp;
+      const float h = to_tf32(acc);
+      hi[o] = h;
+      lo[o] = to_tf32(acc - h);
+    }
+  }
+}
+
+// Z2 (right): CTA = 32 consecutive b' (lanes) x EB consecutive a.
+__global__ void __launch_bounds__(256) env_right_mpo_kernel(const float* __restrict__ Z1, const double* __restrict__ W,
+                                                            int chil, int d, int chir, int wl, int wr, int Kp,
+                                                            float* __restrict__ hi, float* __restrict__ lo) {
+  extern __shared__ float sm[];
+  const int nin = d * wr, nout = wl * d;
+  float* sW = sm;                    // [(k,s')][(s,m)]
+  float* sX = sW + nout * nin;       // [a_local][(s,m)][b_local 32]
+  const int b0 = blockIdx.x * 32, a0 = blockIdx.y * EB;
+  for (int i = threadIdx.x; i < nout * nin; i += blockDim.x) {
+    const int r = i / nin, c = i % nin;
+    const int k = r / d, sp = r % d, s = c / wr, m = c % wr;
+    sW[i] = static_cast<float>(W[((k * d + s) * d + sp) * wr + m]);
+  }
+  const long long ldz = (long long)chir * wr;
+  for (int i = threadIdx.x; i < EB * d * 32 * wr; i += blockDim.x) {
+    const int col = i % (32 * wr);            // (b_local, m) contiguous in Z1
+    const int s = (i / (32 * wr)) % d;
+    const int al = i / (32 * wr * d);
+    const int bl = col / wr, m = col % wr;
+    const int a = a0 + al, b = b0 + bl;
+    float v = 0.f;
+    if (a < chil && b < chir) v = Z1[((long long)a * d + s) * ldz + (long long)b * wr + m];
+    sX[(al * nin + s * wr + m) * 32 + bl] = v;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int b = b0 + lane;
+  for (int row = warp; row < EB * nout; row += 8) {
+    const int al = row / nout, r = row % nout;
+    const int a = a0 + al;
+    if (a >= chil) continue;
+    const float* w = sW + r * nin;
+    const float* x = sX + (al * nin) * 32 + lane;
+    float acc = 0.f;
+    for (int c = 0; c < nin; ++c) acc = fmaf(w[c], x[c * 32], acc);
+    if (b < chir) {
+      const int k = r / d, sp = r % d;
+      const long long o = ((long long)k * chil + a) * Kp + (long long)sp * chir + b;
+      const float h = to_tf32(acc);
+      hi[o] = h;
+      lo[o] = to_tf32(acc - h);
+    }
+  }
+}
+
+struct EnvPlan {
+  int Kp1, Kp2;
+  float *A1hi, *A1lo, *E1hi, *E1lo, *Y1, *Y2hi, *Y2lo, *A2hi, *A2lo;
+  int* err;
+  size_t bytes;
+};
+
+EnvPlan env_plan(int side, int cl, int d, int cr, int wl, int wr, void* work) {
+  EnvPlan p;
+  char* b = static_cast<char*>(work);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    void* q = b ? b + off : nullptr;
+    off += align_up(bytes, 1024);
+    return q;
+  };
+  const size_t f = sizeof(float);
+  p.err = static_cast<int*>(take(256));
+  if (side == 0) {
+    p.Kp1 = pad32(cl);
+    p.Kp2 = pad32((long long)cl * d);
+    p.A1hi = static_cast<float*>(take(f * (size_t)d * cr * p.Kp1));
+    p.A1lo = static_cast<float*>(take(f * (size_t)d * cr * p.Kp1));
+    p.E1hi = static_cast<float*>(take(f * (size_t)cl * wl * p.Kp1));
+    p.E1lo = static_cast<float*>(take(f * (size_t)cl * wl * p.Kp1));
+    p.Y1 = static_cast<float*>(take(f * (size_t)d * cr * cl * wl));
+    p.Y2hi = static_cast<float*>(take(f * (size_t)wr * cr * p.Kp2));
+    p.Y2lo = static_cast<float*>(take(f * (size_t)wr * cr * p.Kp2));
+    p.A2hi = static_cast<float*>(take(f * (size_t)cr * p.Kp2));
+    p.A2lo = static_cast<float*>(take(f * (size_t)cr * p.Kp2));
+  } else {
+    p.Kp1 = pad32(cr);
+    p.Kp2 = pad32((long long)cr * d);
+    p.A1hi = static_cast<float*>(take(f * (size_t)cl * d * p.Kp1));
+    p.A1lo = static_cast<float*>(take(f * (size_t)cl * d * p.Kp1));
+    p.E1hi = static_cast<float*>(take(f * (size_t)cr * wr * p.Kp1));
+    p.E1lo = static_cast<float*>(take(f * (size_t)cr * wr * p.Kp1));
+    p.Y1 = static_cast<float*>(take(f * (size_t)cl * d * cr * wr));
+    p.Y2hi = static_cast<float*>(take(f * (size_t)wl * cl * p.Kp2));
+    p.Y2lo = static_cast<float*>(take(f * (size_t)wl * cl * p.Kp2));
+    p.A2hi = static_cast<float*>(take(f * (size_t)cl * p.Kp2));
+    p.A2lo = static_cast<float*>(take(f * (size_t)cl * p.Kp2));
+  }
+  p.bytes = off;
+  return p;
+}
+
+}  // namespace
+
+size_t tf32x3_env_workspace_bytes(int chil, int d, int chir, int wl, int wr) {
+  size_t a = env_plan(0, chil, d, chir, wl, wr, nullptr).bytes;
+  size_t b = env_plan(1, chil, d, chir, wl, wr, nullptr).bytes;
+  return a > b ? a : b;
+}
+
+int tf32x3_env(int side, int cl, int d, int cr, int wl, int wr, const double* E, const double* W, const double* A,
+               double* Enew, void* work, cudaStream_t s) {
+  EnvPlan p = env_plan(side, cl, d, cr, wl, wr, work);
+  DMRG_CUDA_TRY(cudaMemsetAsync(p.err, 0, 256, s));
+  static bool attr = false;
+  if (!attr) {
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(env_left_mpo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(env_right_mpo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  if (side == 0) {
+    // GEMM 1: rows (s,b) of A^T, cols (a',k) of L, K = a
+    DMRG_TRY(split_transpose(A, (long long)d * cr, cl, d * cr, p.Kp1, p.A1hi, p.A1lo, s));
+    DMRG_TRY(split_rows(E, cl, 1, cl * wl, cl, p.Kp1, p.E1hi, p.E1lo, s));
+    GemmOut g1{p.Y1, (long long)cl * wl, 1, d * cr, cl * wl, 0, 0, 1.f};
+    DMRG_TRY(gemm_split(p.A1hi, p.A1lo, p.E1hi, p.E1lo, d * cr, cl * wl, p.Kp1, g1, p.err, s));
+    // MPO step -> Y2 rows (m,b), K = (a',s')
+    DMRG_CUDA_TRY(cudaMemsetAsync(p.Y2hi, 0, sizeof(float) * (size_t)wr * cr * p.Kp2, s));
+    DMRG_CUDA_TRY(cudaMemsetAsync(p.Y2lo, 0, sizeof(float) * (size_t)wr * cr * p.Kp2, s));
+    const size_t smem = sizeof(float) * ((size_t)d * wr * d * wl + (size_t)EB * d * wl * 32);
+    if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
+    dim3 grid((cl + 31) / 32, (cr + EB - 1) / EB);
+    if (grid.y > 65535) return DMRG_ERR_ARG;
+    env_left_mpo_kernel<<<grid, 256, smem, s>>>(p.Y1, W, cl, d, cr, wl, wr, p.Kp2, p.Y2hi, p.Y2lo);
+    DMRG_CHECK_LAUNCH();
+    // GEMM 2: rows b' of A^T (K = (a',s')), cols (m,b)
+    DMRG_TRY(split_transpose(A, cr, cl * d, cr, p.Kp2, p.A2hi, p.A2lo, s));
+    GemmOut g2{Enew, (long long)wr * cr, 1, cr, wr * cr, 1, 0, 1.f};
+    DMRG_TRY(gemm_split(p.A2hi, p.A2lo, p.Y2hi, p.Y2lo, cr, wr * cr, p.Kp2, g2, p.err, s));
+  } else {
+    // GEMM 1: rows (a,s) of B, cols (b',m) of R, K = b
+    DMRG_TRY(split_rows(A, cr, 1, cl * d, cr, p.Kp1, p.A1hi, p.A1lo, s));
+    DMRG_TRY(split_rows(E, cr, 1, cr * wr, cr, p.Kp1, p.E1hi, p.E1lo, s));
+    GemmOut g1{p.Y1, (long long)cr * wr, 1, cl * d, cr * wr, 0, 0, 1.f};
+    DMRG_TRY(gemm_split(p.A1hi, p.A1lo, p.E1hi, p.E1lo, cl * d, cr * wr, p.Kp1, g1, p.err, s));
+    DMRG_CUDA_TRY(cudaMemsetAsync(p.Y2hi, 0, sizeof(float) * (size_t)wl * cl * p.Kp2, s));
+    DMRG_CUDA_TRY(cudaMemsetAsync(p.Y2lo, 0, sizeof(float) * (size_t)wl * cl * p.Kp2, s));
+    const size_t smem = sizeof(float) * ((size_t)wl * d * d * wr + (size_t)EB * d * wr * 32);
+    if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
+    dim3 grid((cr + 31) / 32, (cl + EB - 1) / EB);
+    if (grid.y > 65535) return DMRG_ERR_ARG;
+    env_right_mpo_kernel<<<grid, 256, smem, s>>>(p.Y1, W, cl, d, cr, wl, wr, p.Kp2, p.Y2hi, p.Y2lo);
+    DMRG_CHECK_LAUNCH();
+    // GEMM 2: rows a' of B (K = (s',b')), cols (k,a)
+    DMRG_TRY(split_rows(A, (long long)d * cr, 1, cl, d * cr, p.Kp2, p.A2hi, p.A2lo, s));
+    GemmOut g2{Enew, (long long)wl * cl, 1, cl, wl * cl, 1, 0, 1.f};
+    DMRG_TRY(gemm_split(p.A2hi, p.A2lo, p.Y2hi, p.Y2lo, cl, wl * cl, p.Kp2, g2, p.err, s));
+  }
+  int h = 0;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(&h, p.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
 
 }  // namespace dmrg

@@ -6,11 +6,27 @@ namespace dmrg {
 
 size_t tf32x3_heff_workspace_bytes(const dmrg_heff_t& o);
 int tf32x3_heff_apply(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s);
+// split L/R and the two-site MPO once per operator; then apply per iteration
+int tf32x3_heff_prepare(const dmrg_heff_t& o, void* work, cudaStream_t s);
+int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s);
+// bounded-wait status recorded by the tcgen05 kernels since the last prepare (syncs the stream)
+int tf32x3_heff_status(const dmrg_heff_t& o, void* work, cudaStream_t s);
 size_t tf32x3_env_workspace_bytes(int chil, int d, int chir, int wl, int wr);
 int tf32x3_env(int side, int chil, int d, int chir, int wl, int wr, const double* E, const double* W, const double* A,
                double* Enew, void* work, cudaStream_t s);
 
 size_t tf32x3_gemm_workspace_bytes(int m, int k, int n);
 int tf32x3_gemm(int m, int k, int n, const double* A, const double* B, double* C, void* work, cudaStream_t s);
+
+// C (m x n, ldc) (+)= alpha op(A) op(B) on split-TF32 tensor cores (see tf32x3.cu)
+size_t tf32x3_gemm_ex_workspace_bytes(int m, int n, int k);
+int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, const double* A, long long lda,
+                   const double* B, long long ldb, int accumulate, double* C, long long ldc, void* work, int* err,
+                   cudaStream_t s);
+
+// warm-started subspace-iteration truncation (subspace.cu)
+size_t subspace_workspace_bytes(int m, int n, int k);
+int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, double* left,
+                      double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s);
 
 }  // namespace dmrg

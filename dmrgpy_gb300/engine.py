@@ -16,6 +16,15 @@ import numpy as np
 from . import _lib
 
 LANCZOS_TOL = 1e-12          # pyitensor/dmrg.py:95
+# With split-TF32 matvecs the operator is applied to ~1e-7 relative accuracy,
+# so successive Ritz values cannot settle to 1e-12; the convergence test
+# then uses this looser relative tolerance (the FP64 refinement step restores
+# FP64 accuracy of the reported energy).
+LANCZOS_TOL_TF32 = 1e-9
+TF32_MIN_CHI = 32            # bonds with a smaller chi stay on the FP64 path
+# split-TF32 sweeps with a maxdim-bound truncation (cutoff <= 0) factorise
+# theta by warm-started subspace iteration once min(m, n) reaches this size
+SUBSPACE_MIN_DIM = 256
 LANCZOS_NITER_FLOOR = 200    # pyitensor/dmrg.py:315-330
 KRYLOV_ERRGOAL = 1e-10       # pyitensor/tdvp.py:79
 KRYLOV_TOL = 1e-12           # pyitensor/tdvp.py:82
@@ -107,15 +116,25 @@ class Engine:
     def to_host(self, tensors):
         return [t.detach().cpu().numpy() for t in tensors]
 
+    def prec_for(self, cl, cr):
+        """Split-TF32 for the bulk bonds, FP64 for the small edge bonds."""
+        if self.prec == _lib.PREC_TF32X3 and min(cl, cr) >= TF32_MIN_CHI:
+            return _lib.PREC_TF32X3
+        return _lib.PREC_FP64
+
     def _heff(self, kind, L, W1, W2, R, cl, d1, d2, cr, wl, wm, wr):
         h = _lib.HeffDesc()
-        h.kind, h.dtype, h.precision = kind, self.cdtype, self.prec
+        h.kind, h.dtype = kind, self.cdtype
+        h.precision = self.prec_for(cl, cr) if kind == 2 else _lib.PREC_FP64
         h.chil, h.d1, h.d2, h.chir = cl, d1, d2, cr
         h.wl, h.wm, h.wr = wl, wm, wr
         h.L = L.data_ptr()
         h.R = R.data_ptr()
         h.W1 = W1.data_ptr() if W1 is not None else None
         h.W2 = W2.data_ptr() if W2 is not None else None
+        # the descriptor holds raw device pointers: keep the tensors alive
+        # for as long as the descriptor is
+        h._keep = (L, W1, W2, R)
         return h
 
     def heff2(self, L, Wi, Wj, R, theta_shape):
@@ -153,8 +172,9 @@ class Engine:
         ptr, size = self.ws.get(need)
         e = ctypes.c_double(0.0)
         it = ctypes.c_int(0)
+        tol = LANCZOS_TOL_TF32 if h.precision == _lib.PREC_TF32X3 else LANCZOS_TOL
         _lib.check("dmrg_lanczos_ground", self.lib.dmrg_lanczos_ground(
-            ctypes.byref(h), x.data_ptr(), k, LANCZOS_TOL, ctypes.byref(e), ctypes.byref(it), ptr, size, self.stream))
+            ctypes.byref(h), x.data_ptr(), k, tol, ctypes.byref(e), ctypes.byref(it), ptr, size, self.stream))
         return e.value, it.value
 
     def expm(self, h, x, coeff, niter):
@@ -175,9 +195,10 @@ class Engine:
         k2, n = B2.shape
         assert k == k2
         C = torch.empty((m, n), dtype=self.tdtype, device=self.device)
-        need = self.lib.dmrg_gemm_workspace_bytes(self.cdtype, self.prec, m, k, n)
+        prec = self.prec_for(min(m, n), k)
+        need = self.lib.dmrg_gemm_workspace_bytes(self.cdtype, prec, m, k, n)
         ptr, size = self.ws.get(need)
-        _lib.check("dmrg_gemm", self.lib.dmrg_gemm(self.cdtype, self.prec, m, k, n, A2.data_ptr(), B2.data_ptr(),
+        _lib.check("dmrg_gemm", self.lib.dmrg_gemm(self.cdtype, prec, m, k, n, A2.data_ptr(), B2.data_ptr(),
                                                    C.data_ptr(), ptr, size, self.stream))
         return C
 
@@ -207,27 +228,49 @@ class Engine:
         k = keep.value
         return lo[:m * k].view(m, k), ro[:k * n].view(k, n), s, k, disc.value
 
-    def env_left(self, L, W, A):
+    def subspace_split(self, M2, k, start, kstart, absorb):
+        """Fixed-rank factorisation of a 2-D device matrix by warm-started
+        subspace iteration (split-TF32): -> (left, right, None, k, disc)."""
+        torch = _torch()
+        m, n = M2.shape
+        lo = torch.empty((m, k), dtype=self.tdtype, device=self.device)
+        ro = torch.empty((k, n), dtype=self.tdtype, device=self.device)
+        disc = ctypes.c_double(0.0)
+        need = self.lib.dmrg_subspace_workspace_bytes(m, n, k)
+        ptr, size = self.ws.get(need)
+        st = self.lib.dmrg_subspace_truncate(m, n, k, M2.data_ptr(), start.data_ptr() if start is not None else None,
+                                             int(kstart), int(absorb), lo.data_ptr(), ro.data_ptr(),
+                                             ctypes.byref(disc), ptr, size, self.stream)
+        _lib.check("dmrg_subspace_truncate", st)
+        return lo, ro, None, k, disc.value
+
+    def use_subspace(self, m, n, cutoff, maxdim):
+        return (self.prec == _lib.PREC_TF32X3 and self.real and cutoff <= 0.0 and maxdim and maxdim > 0
+                and min(m, n) >= SUBSPACE_MIN_DIM)
+
+    def env_left(self, L, W, A, fp64=False):
         torch = _torch()
         cl, d, cr = A.shape
         wl, wr = W.shape[0], W.shape[3]
         out = torch.empty((cr, wr, cr), dtype=self.tdtype, device=self.device)
-        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, self.prec, cl, d, cr, wl, wr)
+        prec = self.prec_for(cl, cr) if fp64 is False else _lib.PREC_FP64
+        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, prec, cl, d, cr, wl, wr)
         ptr, size = self.ws.get(need)
         _lib.check("dmrg_env_extend_left", self.lib.dmrg_env_extend_left(
-            self.cdtype, self.prec, cl, d, cr, wl, wr, L.data_ptr(), W.data_ptr(), A.data_ptr(), out.data_ptr(),
+            self.cdtype, prec, cl, d, cr, wl, wr, L.data_ptr(), W.data_ptr(), A.data_ptr(), out.data_ptr(),
             ptr, size, self.stream))
         return out
 
-    def env_right(self, R, W, B):
+    def env_right(self, R, W, B, fp64=False):
         torch = _torch()
         cl, d, cr = B.shape
         wl, wr = W.shape[0], W.shape[3]
         out = torch.empty((cl, wl, cl), dtype=self.tdtype, device=self.device)
-        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, self.prec, cl, d, cr, wl, wr)
+        prec = self.prec_for(cl, cr) if fp64 is False else _lib.PREC_FP64
+        need = self.lib.dmrg_env_workspace_bytes(self.cdtype, prec, cl, d, cr, wl, wr)
         ptr, size = self.ws.get(need)
         _lib.check("dmrg_env_extend_right", self.lib.dmrg_env_extend_right(
-            self.cdtype, self.prec, cl, d, cr, wl, wr, R.data_ptr(), W.data_ptr(), B.data_ptr(), out.data_ptr(),
+            self.cdtype, prec, cl, d, cr, wl, wr, R.data_ptr(), W.data_ptr(), B.data_ptr(), out.data_ptr(),
             ptr, size, self.stream))
         return out
 
@@ -263,7 +306,20 @@ class Engine:
         energy, k = self.ground(h, theta, niter)
         t2 = time.perf_counter()
         cl, d1, d2, cr = theta.shape
-        lo, ro, s, keep, disc = self.svd(theta.view(cl * d1, d2 * cr), cutoff, maxdim, 1, absorb)
+        m, n = cl * d1, d2 * cr
+        if self.use_subspace(m, n, cutoff, maxdim):
+            k = min(maxdim, m, n)
+            if absorb == 0:
+                start = Ai.reshape(m, Ai.shape[2])
+                kx = min(start.shape[1], k)
+                start = start[:, :kx].contiguous()
+            else:
+                start = Aj.reshape(Aj.shape[0], n)
+                kx = min(start.shape[0], k)
+                start = start[:kx].contiguous()
+            lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), k, start, kx, absorb)
+        else:
+            lo, ro, s, keep, disc = self.svd(theta.view(m, n), cutoff, maxdim, 1, absorb)
         t3 = time.perf_counter()
         st = self.stats
         st.t["merge"] += t1 - t0
@@ -316,6 +372,19 @@ class Engine:
 
     def invalidate(self):
         self._renv = None
+
+    def energy_fp64(self, A):
+        """FP64 refinement of the energy: <psi|H|psi> / <psi|psi> with every
+        environment recomputed in FP64 (used after split-TF32 sweeps)."""
+        torch = _torch()
+        L = self.edge
+        N = self.edge
+        for i, a in enumerate(A):
+            d = a.shape[1]
+            ident = torch.eye(d, dtype=self.tdtype, device=self.device).reshape(1, d, d, 1)
+            L = self.env_left(L, self.W[i], a, fp64=True)
+            N = self.env_left(N, ident.contiguous(), a, fp64=True)
+        return float(L.reshape(-1)[0].real.item() / N.reshape(-1)[0].real.item())
 
     # ------------------------------------------------------------ initial state
     def canonicalize_right_to_left_of(self, A):

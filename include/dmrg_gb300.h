@@ -73,6 +73,9 @@ typedef struct dmrg_heff_t {
 int dmrg_version(void);
 /* Static description of a status code. */
 const char* dmrg_status_string(int status);
+/* Number of CUDA kernels this library has launched in this process (all
+ * devices, all streams); a monotonic counter for instrumentation. */
+unsigned long long dmrg_kernel_launches(void);
 
 /* ---- effective-Hamiltonian matvec ------------------------------------- */
 /* Workspace for dmrg_heff_apply (also covers the operand preparation). */
@@ -82,6 +85,19 @@ size_t dmrg_heff_workspace_bytes(const dmrg_heff_t* op);
  * not alias. */
 int dmrg_heff_apply(const dmrg_heff_t* op, const void* x, void* y,
                     void* work, size_t work_bytes, void* stream);
+
+/* The same matvec split in two, for callers that drive their own Krylov
+ * loop: dmrg_heff_prepare() does the per-operator work once (split-TF32:
+ * splitting L, R and the two-site MPO into the workspace; FP64: nothing),
+ * dmrg_heff_apply_prepared() applies H_eff for each new vector with the same
+ * op and workspace (the plan-once / replay-per-iteration structure of
+ * pyitensor/kernels.py:353-410).  dmrg_heff_status() synchronises the stream
+ * and reports a bounded-wait timeout recorded by the tensor-core kernels
+ * since the last prepare. */
+int dmrg_heff_prepare(const dmrg_heff_t* op, void* work, size_t work_bytes, void* stream);
+int dmrg_heff_apply_prepared(const dmrg_heff_t* op, const void* x, void* y,
+                             void* work, size_t work_bytes, void* stream);
+int dmrg_heff_status(const dmrg_heff_t* op, void* work, size_t work_bytes, void* stream);
 
 /* ---- environments ----------------------------------------------------- */
 size_t dmrg_env_workspace_bytes(int dtype, int precision, int chil, int d, int chir, int wl, int wr);
@@ -138,6 +154,23 @@ int dmrg_svd_truncate(int dtype, int m, int n, const void* M,
                       void* left_out, void* right_out,
                       double* svals, int* keep, double* discarded,
                       void* work, size_t work_bytes, void* stream);
+
+/* Fixed-rank truncation for the split-TF32 sweep when maxdim binds
+ * (cutoff <= 0): keeps k = maxdim vectors found by one warm-started
+ * subspace iteration with block Gram-Schmidt orthonormalisation (all
+ * contractions split-TF32 on tcgen05), instead of a full SVD.  Real dtype.
+ *   absorb 0: left_out (m x k) orthonormal columns, right_out = left^T theta
+ *             (k x n); start = current left tensor as m x kstart (ld kstart)
+ *   absorb 1: right_out (k x n) orthonormal rows, left_out = theta right^T
+ *             (m x k); start = current right tensor as kstart x n
+ * Start vectors beyond kstart are random.  *discarded receives the weight of
+ * theta outside the kept space over |theta|^2.  Stands in for the
+ * maxdim-bound case of pyitensor/svd.py:154-195 as used by
+ * pyitensor/dmrg.py:336-352 (singular values are not formed). */
+size_t dmrg_subspace_workspace_bytes(int m, int n, int k);
+int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* start, int kstart, int absorb,
+                           void* left_out, void* right_out, double* discarded,
+                           void* work, size_t work_bytes, void* stream);
 
 /* ---- dense contraction ---------------------------------------------------- */
 size_t dmrg_gemm_workspace_bytes(int dtype, int precision, int m, int k, int n);

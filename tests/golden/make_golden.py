@@ -257,6 +257,7 @@ def main(ref_root):
     gs("tfim4", [2] * 4, [(-1.0 + 0j, [("Sz", i), ("Sz", i + 1)]) for i in range(1, 4)]
        + [(1.0 + 0j, [("Sx", i)]) for i in range(1, 5)], 16, 6, 2, ed=True)
     gs("s1_heis10_chi32", [3] * 10, terms_heisenberg(10), 32, 6, 3, entropy_bond=5)
+    gs("s1_heis8_chi81", [3] * 8, terms_heisenberg(8), 81, 6, 6, ed=True, entropy_bond=4)
     gs("hub4_chi32", [1] * 4, terms_store["hubbard4"], 32, 6, 4, ed=True)
     gs("spinless8_chi32", [0] * 8, terms_store["spinless8"], 32, 6, 5, ed=True)
 

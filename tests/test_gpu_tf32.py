@@ -1,0 +1,77 @@
+"""Split-TF32 (3 products, FP32 accumulation) tcgen05 path against the FP64
+oracle.  Tolerance: max|y - y_ref| <= 2e-6 * max|y_ref| -- FP32-level, the
+accuracy class of 3xTF32 with FP32 accumulation over K <= ~10^4 terms."""
+import numpy as np
+import pytest
+
+import oracle as O
+from golden_data import terms_heisenberg
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+
+def _engine(W, precision):
+    from dmrgpy_gb300.engine import Engine
+    return Engine(W, real=True, precision=precision)
+
+
+def _mpo_pair(code):
+    from dmrgpy_gb300 import mpo as M
+    W, real = M.build_mpo([code] * 6, terms_heisenberg(6))
+    assert real
+    return W[2], W[3]
+
+
+@pytest.mark.parametrize("chil,chir,code", [(96, 96, 2), (64, 160, 3), (256, 256, 3), (37, 45, 2)])
+def test_tf32x3_two_site_matvec(chil, chir, code):
+    rng = np.random.default_rng(chil * 7 + chir)
+    Wi, Wj = _mpo_pair(code)
+    d, w = Wi.shape[1], Wi.shape[3]
+    L = rng.standard_normal((chil, w, chil))
+    R = rng.standard_normal((chir, w, chir))
+    th = rng.standard_normal((chil, d, d, chir))
+    ref = O.heff2_matvec(L, Wi, Wj, R, th).real
+    eng = _engine([Wi, Wj], "tf32x3")
+    Ld, Rd, thd = eng.to_device([L, R, th])
+    h = eng.heff2(Ld, eng.W[0], eng.W[1], Rd, th.shape)
+    y = eng.apply(h, thd).cpu().numpy()
+    err = np.max(np.abs(y - ref)) / np.max(np.abs(ref))
+    assert err < TOL, err
+    # two applications in a row give identical results (no stale state)
+    y2 = eng.apply(h, thd).cpu().numpy()
+    assert np.array_equal(y, y2)
+
+
+@pytest.mark.parametrize("m,k,n", [(300, 64, 200), (3 * 128, 256, 3 * 128), (5, 7, 9)])
+def test_tf32x3_gemm(m, k, n):
+    rng = np.random.default_rng(m + k + n)
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    eng = _engine([np.zeros((1, 2, 2, 1))], "tf32x3")
+    Ad, Bd = eng.to_device([A, B])
+    C = eng.gemm(Ad, Bd).cpu().numpy()
+    ref = A @ B
+    assert np.max(np.abs(C - ref)) / np.max(np.abs(ref)) < TOL
+
+
+def test_tf32x3_lanczos_energy_close_to_fp64():
+    rng = np.random.default_rng(5)
+    Wi, Wj = _mpo_pair(3)
+    d, w = Wi.shape[1], Wi.shape[3]
+    chi = 128
+    # Hermitian environments: symmetrise random blocks per MPO index
+    L = rng.standard_normal((chi, w, chi))
+    L = 0.5 * (L + L.transpose(2, 1, 0))
+    R = rng.standard_normal((chi, w, chi))
+    R = 0.5 * (R + R.transpose(2, 1, 0))
+    th = rng.standard_normal((chi, d, d, chi))
+    out = {}
+    for prec in ("fp64", "tf32x3"):
+        eng = _engine([Wi, Wj], prec)
+        Ld, Rd, thd = eng.to_device([L, R, th])
+        h = eng.heff2(Ld, eng.W[0], eng.W[1], Rd, th.shape)
+        e, k = eng.ground(h, thd, 200)
+        out[prec] = e
+    assert abs(out["tf32x3"] - out["fp64"]) <= 1e-5 * abs(out["fp64"])

@@ -94,11 +94,12 @@ def _gs(types, terms, maxm, nsweeps, seed):
     return e, psi
 
 
-@pytest.mark.parametrize("tag", ["heis12_chi64", "tfim4", "hub4_chi32", "spinless8_chi32", "s1_heis10_chi32"])
+@pytest.mark.parametrize("tag", ["heis12_chi64", "tfim4", "hub4_chi32", "spinless8_chi32", "s1_heis10_chi32",
+                                 "s1_heis8_chi81"])
 def test_ground_state_energies_match_reference(tag):
     r = META["ground_states"][tag]
     key = {"heis12_chi64": None, "tfim4": None, "hub4_chi32": "hubbard4",
-           "spinless8_chi32": "spinless8", "s1_heis10_chi32": None}[tag]
+           "spinless8_chi32": "spinless8", "s1_heis10_chi32": None, "s1_heis8_chi81": None}[tag]
     if tag == "heis12_chi64":
         types, terms = [2] * 12, terms_heisenberg(12)
     elif tag == "tfim4":
@@ -107,6 +108,8 @@ def test_ground_state_energies_match_reference(tag):
                 [(1.0 + 0j, [("Sx", i)]) for i in range(1, 5)]
     elif tag == "s1_heis10_chi32":
         types, terms = [3] * 10, terms_heisenberg(10)
+    elif tag == "s1_heis8_chi81":
+        types, terms = [3] * 8, terms_heisenberg(8)
     else:
         types, terms = META["types"][key], META["terms"][key]
     e, psi = _gs(types, terms, r["maxm"], r["nsweeps"], r["seed"])
