@@ -66,8 +66,8 @@ SIGNATURES = [
     ("dmrg_svd_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_double, c_int, c_int, c_int,
                                   c_void_p, c_void_p, P_double, P_int, P_double, c_void_p, c_size_t, c_void_p]),
     ("dmrg_subspace_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
-    ("dmrg_subspace_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p,
-                                       P_double, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_subspace_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p,
+                                       c_void_p, P_double, c_void_p, c_size_t, c_void_p]),
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),

@@ -17,7 +17,7 @@ int env_right_fp64(long long cl, long long d, long long cr, long long wl, long l
 
 // truncated SVD (one-sided Jacobi)
 size_t svd_work_bytes(int dtype, int m, int n);
-template <typename T> int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, cudaStream_t s);
+template <typename T> int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, int abs_floor, cudaStream_t s);
 template <typename T> int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s);
 
 // vector ops

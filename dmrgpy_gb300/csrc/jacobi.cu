@@ -69,6 +69,7 @@ struct HArgs {
   unsigned* rotcnt;  // [3], used cyclically: sweep k counts into slot k%3
   int* sweeps_out;
   int X_in_smem;
+  int abs_floor;  // 1: skip couplings below 1e-16 |M|_F^2 (the divided factor is not returned)
 };
 
 template <typename T>
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
     __syncthreads();
   }
   const double fro = *a.frob;
-  const double abs_floor = 1e-16 * fro * fro;
+  const double abs_floor = a.abs_floor ? 1e-16 * fro * fro : 0.0;
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(1024) hestenes_kernel(HArgs<T> a) {
         gre = warp_sum(gre);
         gim = warp_sum(gim);
         double ag = sqrt(gre * gre + gim * gim);
-        double scale = sqrt(al * be);
+        double scale = sqrt(al) * sqrt(be);  // no overflow of the product
         // rotate only couplings above tol relative to the pair and above an
         // absolute floor (1e-16 |M|_F^2): singular values come out to the
         // absolute accuracy of a standard SVD without chasing the relative
@@ -320,11 +321,16 @@ static SvdWork carve(void* work, int dtype, int m, int n) {
   return w;
 }
 
-// Phase 1: factorise.  Leaves sorted singular values in w.sorted (device)
+// Phase 1: factorise.  abs_floor = 1 stops on couplings below 1e-16 |M|_F^2
+// (fewer sweeps on graded spectra): the accumulated rotations stay exactly
+// orthonormal, but the factor formed as X/sigma is then orthonormal only to
+// ~1e-16 |M|^2 / (sigma_p sigma_q); callers enable it only when that factor
+// is not the one that must be orthonormal.
+// Leaves sorted singular values in w.sorted (device)
 // and copies them to host_s.  Returns DMRG_ERR_NOCONV if the sweep limit was
 // reached (the factorisation is still usable).
 template <typename T>
-int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, cudaStream_t s) {
+int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, int abs_floor, cudaStream_t s) {
   const int left = m <= n;
   const int r = left ? n : m;
   const int c = left ? m : n;
@@ -351,6 +357,7 @@ int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* s
   a.sweeps_out = reinterpret_cast<int*>(w.ctrl + 6);
   a.frob = frob;
   a.X_in_smem = 0;
+  a.abs_floor = abs_floor;
   const int half = a.cp / 2;
   // one CTA while the pairs of a round fit in 32 warps of one CTA and the
   // columns are short; otherwise a cooperative grid with one warp per pair
@@ -413,8 +420,8 @@ int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro
   return DMRG_OK;
 }
 
-template int hestenes_factor<double>(const double*, int, int, void*, double*, int*, cudaStream_t);
-template int hestenes_factor<cplx>(const cplx*, int, int, void*, double*, int*, cudaStream_t);
+template int hestenes_factor<double>(const double*, int, int, void*, double*, int*, int, cudaStream_t);
+template int hestenes_factor<cplx>(const cplx*, int, int, void*, double*, int*, int, cudaStream_t);
 template int hestenes_output<double>(int, int, int, int, void*, double*, double*, cudaStream_t);
 template int hestenes_output<cplx>(int, int, int, int, void*, cplx*, cplx*, cudaStream_t);
 

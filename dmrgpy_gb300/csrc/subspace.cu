@@ -20,6 +20,7 @@
 // FP32-level accuracy, which the variational sweep tolerates; energies are
 // refined in FP64 separately.
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "tf32x3.cuh"
@@ -32,118 +33,117 @@ constexpr int PB = 32;   // panel width
 constexpr int CH = 128;  // rows staged per chunk
 
 constexpr int PT = 256;  // threads of the panel kernel
-constexpr int NE = PB * PB / PT;  // Gram entries per thread
 
-// GB300 runs FP64 at 1/64 of the FP32 rate, so the panel arithmetic (Gram
-// products, triangular update) is FP32; the 32x32 Cholesky factor and its
-// inverse are FP64.  Two Cholesky-QR rounds give FP32-level orthonormality.
-__global__ void __launch_bounds__(PT) panel_cholqr2_kernel(double* __restrict__ Z, long long ldz, int m, int c0,
-                                                           int b) {
-  extern __shared__ double sh[];
-  double* G = sh;                                   // PB x (PB+1), FP64
-  double* Ri = G + PB * (PB + 1);                   // PB x (PB+1): inverse factor, FP64
-  float* Rf = reinterpret_cast<float*>(Ri + PB * (PB + 1));  // same, FP32
-  float* tile = Rf + PB * (PB + 1);                 // CH x (PB+1)
-  __shared__ int dead[PB];
-  const int tid = threadIdx.x;
-  const int gj = tid % PB;
-  const int gi = tid / PB;  // rows gi, gi + PT/PB, ...
-  for (int rep = 0; rep < 2; ++rep) {
-    // ---- Gram G = P^T P, two entries per thread (FP32 products, FP64 across chunks)
-    double acc[NE];
+__device__ __forceinline__ float hash_uniform(unsigned long long seed, long long i) {
+  unsigned long long z = seed ^ (0x9e3779b97f4a7c15ull * (unsigned long long)(i + 1));
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  return static_cast<float>((z >> 40) * (1.0 / 16777216.0)) - 0.5f;
+}
+
+// block-wide sum of NV per-thread values (NV <= PB); result in red[0..NV)
+__device__ __forceinline__ void block_sum_vec(float* v, int nv, float* red /* [PT/32][PB] */, float* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = 0; i < nv; ++i) {
+    float x = v[i];
 #pragma unroll
-    for (int e = 0; e < NE; ++e) acc[e] = 0.0;
-    for (int r0 = 0; r0 < m; r0 += CH) {
-      for (int e = tid; e < CH * PB; e += PT) {
-        const int rr = e / PB, cc = e % PB;
-        const int r = r0 + rr;
-        tile[rr * (PB + 1) + cc] = (r < m && cc < b) ? static_cast<float>(Z[(long long)r * ldz + c0 + cc]) : 0.f;
-      }
-      __syncthreads();
-      const int rows = min(CH, m - r0);
-      float pp[NE];
-#pragma unroll
-      for (int e = 0; e < NE; ++e) pp[e] = 0.f;
-      for (int rr = 0; rr < rows; ++rr) {
-        const float xj = tile[rr * (PB + 1) + gj];
-#pragma unroll
-        for (int e = 0; e < NE; ++e) pp[e] = fmaf(tile[rr * (PB + 1) + gi + e * (PT / PB)], xj, pp[e]);
-      }
-#pragma unroll
-      for (int e = 0; e < NE; ++e) acc[e] += pp[e];
-      __syncthreads();
-    }
-#pragma unroll
-    for (int e = 0; e < NE; ++e) {
-      const int r = gi + e * (PT / PB);
-      G[r * (PB + 1) + gj] = (r < b && gj < b) ? acc[e] : (r == gj ? 1.0 : 0.0);
-    }
-    __syncthreads();
-    double tr = 0.0;
-    for (int i = 0; i < b; ++i) tr = fmax(tr, G[i * (PB + 1) + i]);
-    const double floor_ = 1e-12 * tr;   // FP32-level rank threshold
-    // ---- Cholesky G = R^T R in place (upper triangle), right-looking, FP64
-    for (int k = 0; k < PB; ++k) {
-      if (tid == 0) {
-        const double p = G[k * (PB + 1) + k];
-        dead[k] = (k >= b) || !(p > floor_);
-        G[k * (PB + 1) + k] = dead[k] ? 1.0 : sqrt(p);
-      }
-      __syncthreads();
-      const double piv = G[k * (PB + 1) + k];
-      const bool dk = dead[k];
-      if (tid < PB && tid > k) G[k * (PB + 1) + tid] = dk ? 0.0 : G[k * (PB + 1) + tid] / piv;
-      __syncthreads();
-      for (int e = tid; e < PB * PB; e += PT) {
-        const int i = e / PB, j = e % PB;
-        if (i > k && j >= i) G[i * (PB + 1) + j] -= G[k * (PB + 1) + i] * G[k * (PB + 1) + j];
-      }
-      __syncthreads();
-    }
-    // ---- inverse of the upper factor, one column per lane of warp 0 (FP64, stored FP32)
-    if (tid < PB) {
-      const int j = tid;
-      for (int i = 0; i < PB; ++i) Ri[i * (PB + 1) + j] = 0.0;
-      if (!dead[j]) {
-        Ri[j * (PB + 1) + j] = 1.0 / G[j * (PB + 1) + j];
-        for (int i = j - 1; i >= 0; --i) {
-          double s = 0.0;
-          for (int l = i + 1; l <= j; ++l) s += G[i * (PB + 1) + l] * Ri[l * (PB + 1) + j];
-          Ri[i * (PB + 1) + j] = dead[i] ? 0.0 : -s / G[i * (PB + 1) + i];
-        }
-      }
-      for (int i = 0; i < PB; ++i) Rf[i * (PB + 1) + j] = static_cast<float>(Ri[i * (PB + 1) + j]);
-    }
-    __syncthreads();
-    // ---- P <- P R^{-1} row by row in FP32 registers
-    for (int r = tid; r < m; r += PT) {
-      double* zr = Z + (long long)r * ldz + c0;
-      float row[PB];
-#pragma unroll
-      for (int i = 0; i < PB; ++i) row[i] = i < b ? static_cast<float>(zr[i]) : 0.f;
-      // column blocks of 8 in descending order: block jb only reads entries
-      // i < 8*jb + 8, none of which a later (lower) block has overwritten
-#pragma unroll
-      for (int jb = PB / 8 - 1; jb >= 0; --jb) {
-        float o[8];
-#pragma unroll
-        for (int t = 0; t < 8; ++t) o[t] = 0.f;
-#pragma unroll
-        for (int i = 0; i < 8 * jb + 8; ++i) {
-          const float ri = row[i];
-#pragma unroll
-          for (int t = 0; t < 8; ++t)
-            if (i <= 8 * jb + t) o[t] = fmaf(ri, Rf[i * (PB + 1) + 8 * jb + t], o[t]);
-        }
-#pragma unroll
-        for (int t = 0; t < 8; ++t) row[8 * jb + t] = o[t];
-      }
-#pragma unroll
-      for (int j = 0; j < PB; ++j)
-        if (j < b) zr[j] = static_cast<double>(row[j]);
-    }
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp * PB + i] = x;
   }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    float x = 0.f;
+    for (int w = 0; w < PT / 32; ++w) x += red[w * PB + threadIdx.x];
+    out[threadIdx.x] = x;
+  }
+  __syncthreads();
+}
+
+// Column-by-column classical Gram-Schmidt run twice inside one 32-column
+// panel (FP32 arithmetic; GB300 runs FP64 at 1/64 of the FP32 rate).  A column
+// whose norm after the two passes is below `rel` times its reference norm is
+// numerically dependent: mode 0 replaces it by a fresh random vector
+// (orthogonalised the same way), mode 1 zeroes it.  ref2 (b values) holds the
+// reference squared norms; NULL means "the norm on entry".
+__global__ void __launch_bounds__(PT) panel_cgs2_kernel(double* __restrict__ Z, long long ldz, int m, int c0, int b,
+                                                        const double* __restrict__ ref2, float rel, int mode,
+                                                        unsigned long long seed) {
+  __shared__ float red[(PT / 32) * PB];
+  __shared__ float h[PB];
+  __shared__ float nrm[2];
+  float part[PB];
+  for (int j = 0; j < b; ++j) {
+    float ref = 0.f;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      // entry norm
+      float p0 = 0.f;
+      for (int r = threadIdx.x; r < m; r += PT) {
+        const float z = static_cast<float>(Z[(long long)r * ldz + c0 + j]);
+        p0 = fmaf(z, z, p0);
+      }
+      block_sum_vec(&p0, 1, red, nrm);
+      if (attempt == 0) ref = ref2 ? static_cast<float>(ref2[j]) : nrm[0];
+      for (int pass = 0; pass < 2 && j > 0; ++pass) {
+        for (int i = 0; i < j; ++i) part[i] = 0.f;
+        for (int r = threadIdx.x; r < m; r += PT) {
+          const double* zr = Z + (long long)r * ldz + c0;
+          const float zj = static_cast<float>(zr[j]);
+          for (int i = 0; i < j; ++i) part[i] = fmaf(static_cast<float>(zr[i]), zj, part[i]);
+        }
+        block_sum_vec(part, j, red, h);
+        for (int r = threadIdx.x; r < m; r += PT) {
+          double* zr = Z + (long long)r * ldz + c0;
+          float zj = static_cast<float>(zr[j]);
+          for (int i = 0; i < j; ++i) zj = fmaf(-h[i], static_cast<float>(zr[i]), zj);
+          zr[j] = static_cast<double>(zj);
+        }
+        __syncthreads();
+      }
+      float p1 = 0.f;
+      for (int r = threadIdx.x; r < m; r += PT) {
+        const float z = static_cast<float>(Z[(long long)r * ldz + c0 + j]);
+        p1 = fmaf(z, z, p1);
+      }
+      block_sum_vec(&p1, 1, red, nrm);
+      const float n2 = nrm[0];
+      const bool dead = !(n2 > rel * rel * ref) || !(n2 > 1e-30f);
+      if (!dead) {
+        const float inv = rsqrtf(n2);
+        for (int r = threadIdx.x; r < m; r += PT) Z[(long long)r * ldz + c0 + j] *= static_cast<double>(inv);
+        __syncthreads();
+        break;
+      }
+      if (mode == 1 || attempt == 1) {
+        for (int r = threadIdx.x; r < m; r += PT) Z[(long long)r * ldz + c0 + j] = 0.0;
+        __syncthreads();
+        break;
+      }
+      // refill with a random vector and orthogonalise it in the next attempt
+      for (int r = threadIdx.x; r < m; r += PT)
+        Z[(long long)r * ldz + c0 + j] = static_cast<double>(hash_uniform(seed + 7919ull * (c0 + j), r));
+      __syncthreads();
+      ref = 0.f;  // any surviving norm is acceptable for the random vector
+    }
+  }
+}
+
+// squared column norms of Z[:, c0:c0+b]
+__global__ void colnorm2_kernel(const double* __restrict__ Z, long long ldz, int m, int c0, int b,
+                                double* __restrict__ out) {
+  __shared__ float red[(PT / 32) * PB];
+  __shared__ float res[PB];
+  float part[PB];
+  for (int i = 0; i < b; ++i) part[i] = 0.f;
+  for (int r = threadIdx.x; r < m; r += PT) {
+    const double* zr = Z + (long long)r * ldz + c0;
+    for (int i = 0; i < b; ++i) {
+      const float z = static_cast<float>(zr[i]);
+      part[i] = fmaf(z, z, part[i]);
+    }
+  }
+  block_sum_vec(part, b, red, res);
+  if (threadIdx.x < b) out[threadIdx.x] = res[threadIdx.x];
 }
 
 __global__ void random_fill_kernel(double* __restrict__ Z, long long ldz, int m, int c0, int c1, unsigned long long seed) {
@@ -165,6 +165,15 @@ __global__ void copy2d_kernel(const double* __restrict__ src, long long lds, dou
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(i / cols), c = (int)(i % cols);
     dst[(long long)r * ldd + c] = src[(long long)r * lds + c];
+  }
+}
+
+__global__ void copy_scaled_kernel(const double* __restrict__ src, long long lds, double* __restrict__ dst,
+                                   long long ldd, int rows, int cols, double a) {
+  const long long total = (long long)rows * cols;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    dst[(long long)r * ldd + c] = a * src[(long long)r * lds + c];
   }
 }
 
@@ -190,41 +199,54 @@ inline int egrid(long long n) {
   return (int)g;
 }
 
+int copy_scaled(const double* src, long long lds, double* dst, long long ldd, int rows, int cols, double a,
+                cudaStream_t s) {
+  copy_scaled_kernel<<<egrid((long long)rows * cols), 256, 0, s>>>(src, lds, dst, ldd, rows, cols, a);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
 struct OrthWs {
+  double* ref2;  // PB reference squared norms
   double* H;   // k x PB projections
   void* gw;    // split-GEMM scratch
   int* err;
 };
 
 size_t orth_ws_bytes(int m, int k) {
-  return align_up(sizeof(double) * (size_t)k * PB, 1024) + tf32x3_gemm_ex_workspace_bytes(m > k ? m : k, m > k ? m : k, m > k ? m : k) +
+  return align_up(sizeof(double) * PB, 1024) + align_up(sizeof(double) * (size_t)k * PB, 1024) + tf32x3_gemm_ex_workspace_bytes(m > k ? m : k, m > k ? m : k, m > k ? m : k) +
          align_up(256, 1024);
 }
 
-// Z (m x k, row-major, ld) -> orthonormal columns (zero columns for null directions)
+// Z (m x k, row-major, ld) -> orthonormal columns, by block classical
+// Gram-Schmidt run twice (BCGS2): per 32-column panel, [project against the
+// finished panels, orthonormalise inside the panel] twice.  Projections are
+// split-TF32 GEMMs.  Columns that turn out numerically dependent on earlier
+// ones are replaced by random directions in the first round and zeroed if
+// still dependent in the second.
 int orth_bcgs2(double* Z, long long ld, int m, int k, const OrthWs& w, cudaStream_t s) {
-  static bool attr = false;
-  const size_t smem = 2 * sizeof(double) * (size_t)PB * (PB + 1) + sizeof(float) * ((size_t)PB * (PB + 1) + (size_t)CH * (PB + 1));
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(panel_cholqr2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
   for (int c0 = 0; c0 < k; c0 += PB) {
     const int b = (k - c0) < PB ? (k - c0) : PB;
-    if (c0 > 0) {
-      for (int pass = 0; pass < 2; ++pass) {
+    colnorm2_kernel<<<1, PT, 0, s>>>(Z, ld, m, c0, b, w.ref2);
+    DMRG_CHECK_LAUNCH();
+    for (int pass = 0; pass < 2; ++pass) {
+      if (c0 > 0) {
         // H = Q^T Z_j  (c0 x b),  Z_j -= Q H
         DMRG_TRY(tf32x3_gemm_ex(1, 0, c0, b, m, 1.f, Z, ld, Z + c0, ld, 0, w.H, PB, w.gw, w.err, s));
         DMRG_TRY(tf32x3_gemm_ex(0, 0, m, b, c0, -1.f, Z, ld, w.H, PB, 1, Z + c0, ld, w.gw, w.err, s));
       }
+      // round 1: dependent relative to the norm before any projection (1e-5,
+      // above the FP32-level projection error) -> random refill; round 2:
+      // the columns enter with unit norm, dependent -> zero
+      panel_cgs2_kernel<<<1, PT, 0, s>>>(Z, ld, m, c0, b, pass == 0 ? w.ref2 : nullptr, pass == 0 ? 1e-5f : 1e-3f,
+                                          pass, 0x0c0ffee5eedULL + (unsigned long long)c0);
+      DMRG_CHECK_LAUNCH();
     }
-    panel_cholqr2_kernel<<<1, PT, smem, s>>>(Z, ld, m, c0, b);
-    DMRG_CHECK_LAUNCH();
   }
   return DMRG_OK;
 }
 
-// dst (cols x rows, ld = rows) = src^T, src rows x cols with leading dim lds
+// dst (cols x rows, ld = ldd) = src^T, src rows x cols with leading dim lds
 __global__ void transpose_kernel(const double* __restrict__ src, long long lds, int rows, int cols,
                                  double* __restrict__ dst, long long ldd) {
   __shared__ double t[32][33];
@@ -249,22 +271,127 @@ int transpose(const double* src, long long lds, int rows, int cols, double* dst,
   return DMRG_OK;
 }
 
+// ---------------------------------------------------------------- polar orthonormalisation
+// Orthonormal basis of range(Z) as the polar factor of Z, by Newton-Schulz
+// iterations that use only (split-TF32) GEMMs:
+//   columns scaled to unit norm, then /sqrt(k) so every singular value <= 1;
+//   quintic steps X <- aX + X(bA + cA^2), A = X^T X, with (a,b,c) chosen so
+//   that small singular values grow by ~3.4x per step while all stay in
+//   (0, 1.3);
+//   cubic steps X <- X(1.5 I - 0.5 A) until max|A - I| < tol.
+// Directions of Z at the FP32 noise level (or exactly dependent ones, after
+// a tiny random perturbation) become orthonormal completions, so the result
+// is orthonormal whatever the conditioning of Z.
+
+__global__ void scale_cols_kernel(double* __restrict__ Z, long long ld, int m, int k, const double* __restrict__ n2,
+                                  double extra) {
+  const long long total = (long long)m * k;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / k), c = (int)(i % k);
+    const double nn = n2[c];
+    Z[(long long)r * ld + c] = nn > 0.0 ? Z[(long long)r * ld + c] * (extra / sqrt(nn)) : 0.0;
+  }
+}
+
+// n2[c] = sum_r Z[r][c]^2, one warp per column group
+__global__ void colsq_kernel(const double* __restrict__ Z, long long ld, int m, int k, double* __restrict__ n2) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  double s = 0.0;
+  for (int r = 0; r < m; ++r) {
+    const double z = Z[(long long)r * ld + c];
+    s = fma(z, z, s);
+  }
+  n2[c] = s;
+}
+
+// Z += eps * (random), keeps exactly dependent directions from staying at 0
+__global__ void perturb_kernel(double* __restrict__ Z, long long ld, int m, int k, double eps, unsigned long long seed) {
+  const long long total = (long long)m * k;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / k), c = (int)(i % k);
+    Z[(long long)r * ld + c] += eps * static_cast<double>(hash_uniform(seed, i));
+  }
+}
+
+// B = b*A + c*I  (k x k), also reports max|A - I| into *dev
+__global__ void poly_kernel(const double* __restrict__ A, int k, double b, double c, double* __restrict__ B,
+                            unsigned long long* __restrict__ dev) {
+  const long long total = (long long)k * k;
+  double mx = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / k), cc = (int)(i % k);
+    const double a = A[i];
+    B[i] = b * a + (r == cc ? c : 0.0);
+    mx = fmax(mx, fabs(a - (r == cc ? 1.0 : 0.0)));
+  }
+  // max of non-negative doubles via their bit patterns
+  atomicMax(dev, __double_as_longlong(mx));
+}
+
+int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
+               unsigned long long* dev, void* gw, int* err, cudaStream_t s) {
+  // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
+  colsq_kernel<<<(k + 255) / 256, 256, 0, s>>>(Z, ld, m, k, n2);
+  DMRG_CHECK_LAUNCH();
+  scale_cols_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, n2, 1.0 / sqrt((double)k));
+  DMRG_CHECK_LAUNCH();
+  perturb_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, 1e-8 / sqrt((double)m), 0x5eed5ull + (unsigned)k);
+  DMRG_CHECK_LAUNCH();
+  double* X = Z;
+  double* Y = X2;
+  const int quintic = 20, cubic_max = 10;
+  for (int it = 0; it < quintic + cubic_max; ++it) {
+    const bool q = it < quintic;
+    // A = X^T X
+    DMRG_TRY(tf32x3_gemm_ex(1, 0, k, k, m, 1.f, X, ld, X, ld, 0, A, k, gw, err, s));
+    DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+    if (q) {
+      // B = b A + c A^2 ;  X <- a X + X B
+      const double a = 3.4445, b = -4.7750, c = 2.0315;
+      poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, b, 0.0, B, dev);
+      DMRG_CHECK_LAUNCH();
+      DMRG_TRY(tf32x3_gemm_ex(0, 0, k, k, k, (float)c, A, k, A, k, 1, B, k, gw, err, s));
+      // Y = a X ; Y += X B
+      DMRG_TRY(copy_scaled(X, ld, Y, ld, m, k, a, s));
+      DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, X, ld, B, k, 1, Y, ld, gw, err, s));
+    } else {
+      // convergence check on A, then X <- X (1.5 I - 0.5 A)
+      poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, B, dev);
+      DMRG_CHECK_LAUNCH();
+      unsigned long long h = 0;
+      DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
+      DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+      double d;
+      memcpy(&d, &h, sizeof(d));
+      if (d < 5e-6) break;
+      DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, X, ld, B, k, 0, Y, ld, gw, err, s));
+    }
+    double* t = X;
+    X = Y;
+    Y = t;
+  }
+  if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
+  return DMRG_OK;
+}
+
 }  // namespace
 
 size_t subspace_workspace_bytes(int m, int n, int k) {
   const size_t big = (size_t)(m > n ? m : n);
   const size_t d = sizeof(double);
-  return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 4 * align_up(d * big * k, 1024) +
-         orth_ws_bytes((int)big, k) + tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big) + align_up(64, 1024);
+  return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 5 * align_up(d * big * k, 1024) +
+         2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) + orth_ws_bytes((int)big, k) +
+         tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big) + align_up(64, 1024);
 }
 
 // theta (m x n row-major).  absorb 0 keeps an orthonormal LEFT basis; X is
 // the start basis m x kx (ld kx).  absorb 1 keeps an orthonormal RIGHT basis;
 // X is kx x n (ld n).  k vectors are kept; start columns beyond kx are random.
 // Outputs: left (m x k), right (k x n), *disc = discarded weight fraction.
-int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, double* left,
-                      double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s) {
-  if (k <= 0 || k > m || k > n || kx < 0 || kx > k) return DMRG_ERR_ARG;
+int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,
+                      double* left, double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s) {
+  if (k <= 0 || k > m || k > n || kx < 0 || kx > k || iters < 1 || iters > 8) return DMRG_ERR_ARG;
   if (subspace_workspace_bytes(m, n, k) > work_bytes) return DMRG_ERR_WORKSPACE;
   const size_t big = (size_t)(m > n ? m : n);
   const size_t d = sizeof(double);
@@ -275,15 +402,24 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   double* Y = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* C = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* Xs = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
+  double* PX = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
+  double* PA = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
+  double* PB_ = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
+  double* Pn2 = reinterpret_cast<double*>(p); p += align_up(d * k, 1024);
   OrthWs ow;
-  ow.H = reinterpret_cast<double*>(p);
-  ow.gw = p + align_up(sizeof(double) * (size_t)k * PB, 1024);
+  ow.ref2 = reinterpret_cast<double*>(p);
+  ow.H = reinterpret_cast<double*>(p + align_up(sizeof(double) * PB, 1024));
+  ow.gw = p + align_up(sizeof(double) * PB, 1024) + align_up(sizeof(double) * (size_t)k * PB, 1024);
   ow.err = err;
   p += orth_ws_bytes((int)big, k);
   void* gw = p; p += tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big);
   double* acc = reinterpret_cast<double*>(p);
+  unsigned long long* pdev = reinterpret_cast<unsigned long long*>(acc + 4);
   DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, 256, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(acc, 0, 64, s));
+  auto orth = [&](double* Zp, int rows) -> int {
+    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, err, s);
+  };
 
   // canonical problem: keep the left basis of Th (M x N)
   const double* Th = theta;
@@ -304,12 +440,14 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
     random_fill_kernel<<<egrid((long long)M * (k - kx)), 256, 0, s>>>(S, k, M, kx, k, 0x51ab5eedULL + (unsigned)M);
     DMRG_CHECK_LAUNCH();
   }
-  // Y = Th^T S (N x k), W = orth(Y)
-  DMRG_TRY(tf32x3_gemm_ex(1, 0, N, k, M, 1.f, Th, N, S, k, 0, Y, k, gw, err, s));
-  DMRG_TRY(orth_bcgs2(Y, k, N, k, ow, s));
-  // Z = Th W (M x k), Q = orth(Z)  (into S)
-  DMRG_TRY(tf32x3_gemm_ex(0, 0, M, k, N, 1.f, Th, N, Y, k, 0, S, k, gw, err, s));
-  DMRG_TRY(orth_bcgs2(S, k, M, k, ow, s));
+  for (int it = 0; it < iters; ++it) {
+    // Y = Th^T S (N x k), W = orth(Y)
+    DMRG_TRY(tf32x3_gemm_ex(1, 0, N, k, M, 1.f, Th, N, S, k, 0, Y, k, gw, err, s));
+    DMRG_TRY(orth(Y, N));
+    // Z = Th W (M x k), Q = orth(Z)  (into S)
+    DMRG_TRY(tf32x3_gemm_ex(0, 0, M, k, N, 1.f, Th, N, Y, k, 0, S, k, gw, err, s));
+    DMRG_TRY(orth(S, M));
+  }
   // C = Q^T Th (k x N)
   DMRG_TRY(tf32x3_gemm_ex(1, 0, k, N, M, 1.f, S, k, Th, N, 0, C, N, gw, err, s));
   sumsq_kernel<<<egrid((long long)k * N), 256, 0, s>>>(C, (long long)k * N, acc);

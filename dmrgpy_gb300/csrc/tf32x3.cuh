@@ -26,7 +26,7 @@ int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, con
 
 // warm-started subspace-iteration truncation (subspace.cu)
 size_t subspace_workspace_bytes(int m, int n, int k);
-int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, double* left,
-                      double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s);
+int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,
+                      double* left, double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s);
 
 }  // namespace dmrg

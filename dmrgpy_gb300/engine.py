@@ -94,6 +94,8 @@ class Engine:
         self.krylov_budget = krylov_budget_bytes
         self.stats = SweepStats()
         self._renv = None  # right environments valid for the current MPS (after a RL pass)
+        self.subspace_iters = 1     # subspace iterations per fixed-rank truncation
+        self.lanczos_tol_tf32 = LANCZOS_TOL_TF32
 
     # ------------------------------------------------------------ plumbing
     @property
@@ -172,7 +174,7 @@ class Engine:
         ptr, size = self.ws.get(need)
         e = ctypes.c_double(0.0)
         it = ctypes.c_int(0)
-        tol = LANCZOS_TOL_TF32 if h.precision == _lib.PREC_TF32X3 else LANCZOS_TOL
+        tol = self.lanczos_tol_tf32 if h.precision == _lib.PREC_TF32X3 else LANCZOS_TOL
         _lib.check("dmrg_lanczos_ground", self.lib.dmrg_lanczos_ground(
             ctypes.byref(h), x.data_ptr(), k, tol, ctypes.byref(e), ctypes.byref(it), ptr, size, self.stream))
         return e.value, it.value
@@ -239,7 +241,8 @@ class Engine:
         need = self.lib.dmrg_subspace_workspace_bytes(m, n, k)
         ptr, size = self.ws.get(need)
         st = self.lib.dmrg_subspace_truncate(m, n, k, M2.data_ptr(), start.data_ptr() if start is not None else None,
-                                             int(kstart), int(absorb), lo.data_ptr(), ro.data_ptr(),
+                                             int(kstart), int(absorb), int(self.subspace_iters),
+                                             lo.data_ptr(), ro.data_ptr(),
                                              ctypes.byref(disc), ptr, size, self.stream)
         _lib.check("dmrg_subspace_truncate", st)
         return lo, ro, None, k, disc.value
@@ -390,12 +393,18 @@ class Engine:
     def canonicalize_right_to_left_of(self, A):
         """Lossless left-to-right SVD pass (centre ends at the last site) and
         normalisation: pyitensor/mpsalgebra.py:347-352 (position(n), normalize)."""
+        torch = _torch()
         n = len(A)
         for i in range(n - 1):
             cl, d, cr = A[i].shape
             lo, ro, s, keep, _ = self.svd(A[i].reshape(cl * d, cr), 0.0, 0, 1, 0)
             A[i] = lo.reshape(cl, d, keep)
-            A[i + 1] = self.gemm(ro, A[i + 1].reshape(cr, -1)).reshape(keep, A[i + 1].shape[1], A[i + 1].shape[2])
+            nxt = self.gemm(ro, A[i + 1].reshape(cr, -1))
+            # the carried centre grows by ~|A| per site (1e100 and more over a
+            # long chain); its scale is irrelevant because the state is
+            # normalised at the end, so keep it O(1)
+            nxt = nxt / torch.linalg.vector_norm(nxt)
+            A[i + 1] = nxt.reshape(keep, A[i + 1].shape[1], A[i + 1].shape[2])
         nrm = float(_torch().linalg.vector_norm(A[n - 1]).item())
         A[n - 1] = A[n - 1] / nrm
         return A

@@ -163,13 +163,14 @@ int dmrg_svd_truncate(int dtype, int m, int n, const void* M,
  *             (k x n); start = current left tensor as m x kstart (ld kstart)
  *   absorb 1: right_out (k x n) orthonormal rows, left_out = theta right^T
  *             (m x k); start = current right tensor as kstart x n
- * Start vectors beyond kstart are random.  *discarded receives the weight of
+ * Start vectors beyond kstart are random; iters (1..8) subspace iterations
+ * are run.  *discarded receives the weight of
  * theta outside the kept space over |theta|^2.  Stands in for the
  * maxdim-bound case of pyitensor/svd.py:154-195 as used by
  * pyitensor/dmrg.py:336-352 (singular values are not formed). */
 size_t dmrg_subspace_workspace_bytes(int m, int n, int k);
 int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* start, int kstart, int absorb,
-                           void* left_out, void* right_out, double* discarded,
+                           int iters, void* left_out, void* right_out, double* discarded,
                            void* work, size_t work_bytes, void* stream);
 
 /* ---- dense contraction ---------------------------------------------------- */
