@@ -56,6 +56,9 @@ SIGNATURES = [
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     ("dmrg_env_extend_right", c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_env_gradient_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int]),
+    ("dmrg_env_gradient", c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  c_void_p, c_size_t, c_void_p]),
     ("dmrg_lanczos_workspace_bytes", c_size_t, [ctypes.POINTER(HeffDesc), c_int]),
     ("dmrg_lanczos_ground", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_int, c_double, P_double, P_int,
                                     c_void_p, c_size_t, c_void_p]),

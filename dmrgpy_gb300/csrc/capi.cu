@@ -158,9 +158,6 @@ int lowest_ritz(const std::vector<double>& al, const std::vector<double>& be, do
   return DMRG_OK;
 }
 
-// relative accuracy class of a split-TF32 H_eff application (measured
-// ~6e-7 norm-wise at chi=1024) times a safety factor of ~5
-constexpr double kTf32NoiseFloor = 3e-6;
 
 // ---- workspace layout of the Krylov drivers
 struct KrylovWs {
@@ -263,22 +260,7 @@ int lanczos_impl(const dmrg_heff_t* o, T* x, int niter, double tol, double* ener
     beta = hbuf[2];
     k = j + 1;
     double cur;
-    if (o->precision == DMRG_PREC_TF32X3) {
-      // The split-TF32 operator is accurate to ~1e-6 relative, so Ritz values
-      // stop settling at that level; stop instead once the Ritz residual
-      // beta_k |y_k| reaches a few times that noise floor (relative to the
-      // spectral scale of T), or on the Ritz test itself.
-      std::vector<double> y;
-      double lo_ev, scale = 0.0;
-      DMRG_TRY(lowest_ritz(al, be, &cur, &y));
-      lo_ev = cur;
-      for (double a : al) scale = std::max(scale, std::fabs(a));
-      scale = std::max(scale, std::fabs(lo_ev));
-      const double resid = beta * std::fabs(y[k - 1]);
-      if (resid < kTf32NoiseFloor * std::max(1.0, scale)) break;
-    } else {
-      DMRG_TRY(lowest_ritz(al, be, &cur, nullptr));
-    }
+    DMRG_TRY(lowest_ritz(al, be, &cur, nullptr));
     if (std::fabs(cur - prev) < tol * std::max(1.0, std::fabs(cur))) break;
     prev = cur;
   }

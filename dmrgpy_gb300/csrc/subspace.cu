@@ -1,7 +1,7 @@
 // Truncation of a two-site tensor by warm-started subspace iteration, for
 // the split-TF32 sweep at large bond dimension when the kept dimension is
 // fixed by maxdim (cutoff <= 0): no eigensolver, only GEMMs on the tensor
-// cores plus one small Cholesky per 32-column panel.
+// cores plus one FP64 Gram matrix.
 //
 //   keep the left factor (absorb 0):
 //     Y = theta^T X      X: m x k start basis (the current left site tensor)
@@ -12,13 +12,11 @@
 //   keep the right factor (absorb 1): the same on theta^T, returning
 //     left = theta Q (m x k) and right = Q^T (k x n, orthonormal rows).
 //
-// orth() is block classical Gram-Schmidt run twice (BCGS2): each 32-column
-// panel is projected against the finished panels twice (split-TF32 GEMMs)
-// and then orthonormalised by two rounds of Cholesky-QR in FP64 inside one
-// CTA.  Columns whose remaining norm falls below 1e-13 of the panel are
-// zeroed (they carry no weight of theta).  The result is orthonormal to
-// FP32-level accuracy, which the variational sweep tolerates; energies are
-// refined in FP64 separately.
+// orth() is the polar factor of the block by Newton-Schulz iterations, which
+// are GEMMs only (split-TF32 on the tensor cores); the final left/right basis
+// gets one more correction from an FP64 Gram matrix so that it is orthonormal
+// to ~1e-11 (a basis that is only FP32-orthonormal lets the norm environment
+// drift along the chain).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -29,121 +27,12 @@ namespace dmrg {
 
 namespace {
 
-constexpr int PB = 32;   // panel width
-constexpr int CH = 128;  // rows staged per chunk
-
-constexpr int PT = 256;  // threads of the panel kernel
-
 __device__ __forceinline__ float hash_uniform(unsigned long long seed, long long i) {
   unsigned long long z = seed ^ (0x9e3779b97f4a7c15ull * (unsigned long long)(i + 1));
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
   z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
   z ^= z >> 31;
   return static_cast<float>((z >> 40) * (1.0 / 16777216.0)) - 0.5f;
-}
-
-// block-wide sum of NV per-thread values (NV <= PB); result in red[0..NV)
-__device__ __forceinline__ void block_sum_vec(float* v, int nv, float* red /* [PT/32][PB] */, float* out) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i = 0; i < nv; ++i) {
-    float x = v[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) red[warp * PB + i] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < nv) {
-    float x = 0.f;
-    for (int w = 0; w < PT / 32; ++w) x += red[w * PB + threadIdx.x];
-    out[threadIdx.x] = x;
-  }
-  __syncthreads();
-}
-
-// Column-by-column classical Gram-Schmidt run twice inside one 32-column
-// panel (FP32 arithmetic; GB300 runs FP64 at 1/64 of the FP32 rate).  A column
-// whose norm after the two passes is below `rel` times its reference norm is
-// numerically dependent: mode 0 replaces it by a fresh random vector
-// (orthogonalised the same way), mode 1 zeroes it.  ref2 (b values) holds the
-// reference squared norms; NULL means "the norm on entry".
-__global__ void __launch_bounds__(PT) panel_cgs2_kernel(double* __restrict__ Z, long long ldz, int m, int c0, int b,
-                                                        const double* __restrict__ ref2, float rel, int mode,
-                                                        unsigned long long seed) {
-  __shared__ float red[(PT / 32) * PB];
-  __shared__ float h[PB];
-  __shared__ float nrm[2];
-  float part[PB];
-  for (int j = 0; j < b; ++j) {
-    float ref = 0.f;
-    for (int attempt = 0; attempt < 2; ++attempt) {
-      // entry norm
-      float p0 = 0.f;
-      for (int r = threadIdx.x; r < m; r += PT) {
-        const float z = static_cast<float>(Z[(long long)r * ldz + c0 + j]);
-        p0 = fmaf(z, z, p0);
-      }
-      block_sum_vec(&p0, 1, red, nrm);
-      if (attempt == 0) ref = ref2 ? static_cast<float>(ref2[j]) : nrm[0];
-      for (int pass = 0; pass < 2 && j > 0; ++pass) {
-        for (int i = 0; i < j; ++i) part[i] = 0.f;
-        for (int r = threadIdx.x; r < m; r += PT) {
-          const double* zr = Z + (long long)r * ldz + c0;
-          const float zj = static_cast<float>(zr[j]);
-          for (int i = 0; i < j; ++i) part[i] = fmaf(static_cast<float>(zr[i]), zj, part[i]);
-        }
-        block_sum_vec(part, j, red, h);
-        for (int r = threadIdx.x; r < m; r += PT) {
-          double* zr = Z + (long long)r * ldz + c0;
-          float zj = static_cast<float>(zr[j]);
-          for (int i = 0; i < j; ++i) zj = fmaf(-h[i], static_cast<float>(zr[i]), zj);
-          zr[j] = static_cast<double>(zj);
-        }
-        __syncthreads();
-      }
-      float p1 = 0.f;
-      for (int r = threadIdx.x; r < m; r += PT) {
-        const float z = static_cast<float>(Z[(long long)r * ldz + c0 + j]);
-        p1 = fmaf(z, z, p1);
-      }
-      block_sum_vec(&p1, 1, red, nrm);
-      const float n2 = nrm[0];
-      const bool dead = !(n2 > rel * rel * ref) || !(n2 > 1e-30f);
-      if (!dead) {
-        const float inv = rsqrtf(n2);
-        for (int r = threadIdx.x; r < m; r += PT) Z[(long long)r * ldz + c0 + j] *= static_cast<double>(inv);
-        __syncthreads();
-        break;
-      }
-      if (mode == 1 || attempt == 1) {
-        for (int r = threadIdx.x; r < m; r += PT) Z[(long long)r * ldz + c0 + j] = 0.0;
-        __syncthreads();
-        break;
-      }
-      // refill with a random vector and orthogonalise it in the next attempt
-      for (int r = threadIdx.x; r < m; r += PT)
-        Z[(long long)r * ldz + c0 + j] = static_cast<double>(hash_uniform(seed + 7919ull * (c0 + j), r));
-      __syncthreads();
-      ref = 0.f;  // any surviving norm is acceptable for the random vector
-    }
-  }
-}
-
-// squared column norms of Z[:, c0:c0+b]
-__global__ void colnorm2_kernel(const double* __restrict__ Z, long long ldz, int m, int c0, int b,
-                                double* __restrict__ out) {
-  __shared__ float red[(PT / 32) * PB];
-  __shared__ float res[PB];
-  float part[PB];
-  for (int i = 0; i < b; ++i) part[i] = 0.f;
-  for (int r = threadIdx.x; r < m; r += PT) {
-    const double* zr = Z + (long long)r * ldz + c0;
-    for (int i = 0; i < b; ++i) {
-      const float z = static_cast<float>(zr[i]);
-      part[i] = fmaf(z, z, part[i]);
-    }
-  }
-  block_sum_vec(part, b, red, res);
-  if (threadIdx.x < b) out[threadIdx.x] = res[threadIdx.x];
 }
 
 __global__ void random_fill_kernel(double* __restrict__ Z, long long ldz, int m, int c0, int c1, unsigned long long seed) {
@@ -203,46 +92,6 @@ int copy_scaled(const double* src, long long lds, double* dst, long long ldd, in
                 cudaStream_t s) {
   copy_scaled_kernel<<<egrid((long long)rows * cols), 256, 0, s>>>(src, lds, dst, ldd, rows, cols, a);
   DMRG_CHECK_LAUNCH();
-  return DMRG_OK;
-}
-
-struct OrthWs {
-  double* ref2;  // PB reference squared norms
-  double* H;   // k x PB projections
-  void* gw;    // split-GEMM scratch
-  int* err;
-};
-
-size_t orth_ws_bytes(int m, int k) {
-  return align_up(sizeof(double) * PB, 1024) + align_up(sizeof(double) * (size_t)k * PB, 1024) + tf32x3_gemm_ex_workspace_bytes(m > k ? m : k, m > k ? m : k, m > k ? m : k) +
-         align_up(256, 1024);
-}
-
-// Z (m x k, row-major, ld) -> orthonormal columns, by block classical
-// Gram-Schmidt run twice (BCGS2): per 32-column panel, [project against the
-// finished panels, orthonormalise inside the panel] twice.  Projections are
-// split-TF32 GEMMs.  Columns that turn out numerically dependent on earlier
-// ones are replaced by random directions in the first round and zeroed if
-// still dependent in the second.
-int orth_bcgs2(double* Z, long long ld, int m, int k, const OrthWs& w, cudaStream_t s) {
-  for (int c0 = 0; c0 < k; c0 += PB) {
-    const int b = (k - c0) < PB ? (k - c0) : PB;
-    colnorm2_kernel<<<1, PT, 0, s>>>(Z, ld, m, c0, b, w.ref2);
-    DMRG_CHECK_LAUNCH();
-    for (int pass = 0; pass < 2; ++pass) {
-      if (c0 > 0) {
-        // H = Q^T Z_j  (c0 x b),  Z_j -= Q H
-        DMRG_TRY(tf32x3_gemm_ex(1, 0, c0, b, m, 1.f, Z, ld, Z + c0, ld, 0, w.H, PB, w.gw, w.err, s));
-        DMRG_TRY(tf32x3_gemm_ex(0, 0, m, b, c0, -1.f, Z, ld, w.H, PB, 1, Z + c0, ld, w.gw, w.err, s));
-      }
-      // round 1: dependent relative to the norm before any projection (1e-5,
-      // above the FP32-level projection error) -> random refill; round 2:
-      // the columns enter with unit norm, dependent -> zero
-      panel_cgs2_kernel<<<1, PT, 0, s>>>(Z, ld, m, c0, b, pass == 0 ? w.ref2 : nullptr, pass == 0 ? 1e-5f : 1e-3f,
-                                          pass, 0x0c0ffee5eedULL + (unsigned long long)c0);
-      DMRG_CHECK_LAUNCH();
-    }
-  }
   return DMRG_OK;
 }
 
@@ -330,7 +179,7 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
 }
 
 int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
-               unsigned long long* dev, void* gw, int* err, cudaStream_t s) {
+               unsigned long long* dev, void* gw, int* err, bool exact, cudaStream_t s) {
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
   colsq_kernel<<<(k + 255) / 256, 256, 0, s>>>(Z, ld, m, k, n2);
   DMRG_CHECK_LAUNCH();
@@ -372,6 +221,25 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
     Y = t;
   }
   if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
+  if (exact) {
+    // The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
+    // what a product accurate to ~5e-7 can resolve.  A left basis that is
+    // only that orthonormal makes the norm environment drift by ~N x 1e-6
+    // over a chain, so the kept basis gets one correction with an FP64 Gram:
+    //   E = X^T X - I (FP64),  X <- X (I - E/2)   (residual O(E^2)),
+    // where the product X (E/2) only needs the split-TF32 relative accuracy
+    // because E is already tiny.
+    TGemm g{};
+    g.B = ax(1); g.M = ax(k); g.K = ax(m); g.N = ax(k);
+    g.a_m = st(1); g.a_k = st(ld);
+    g.b_k = st(ld); g.b_n = st(1);
+    g.c_m = st(k); g.c_n = st(1);
+    DMRG_TRY(tgemm<double>(g, 1.0, Z, Z, 0.0, A, s));
+    DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+    poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
+    DMRG_CHECK_LAUNCH();
+    DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s));
+  }
   return DMRG_OK;
 }
 
@@ -381,7 +249,7 @@ size_t subspace_workspace_bytes(int m, int n, int k) {
   const size_t big = (size_t)(m > n ? m : n);
   const size_t d = sizeof(double);
   return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 5 * align_up(d * big * k, 1024) +
-         2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) + orth_ws_bytes((int)big, k) +
+         2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) +
          tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big) + align_up(64, 1024);
 }
 
@@ -406,19 +274,13 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   double* PA = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* PB_ = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* Pn2 = reinterpret_cast<double*>(p); p += align_up(d * k, 1024);
-  OrthWs ow;
-  ow.ref2 = reinterpret_cast<double*>(p);
-  ow.H = reinterpret_cast<double*>(p + align_up(sizeof(double) * PB, 1024));
-  ow.gw = p + align_up(sizeof(double) * PB, 1024) + align_up(sizeof(double) * (size_t)k * PB, 1024);
-  ow.err = err;
-  p += orth_ws_bytes((int)big, k);
   void* gw = p; p += tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big);
   double* acc = reinterpret_cast<double*>(p);
   unsigned long long* pdev = reinterpret_cast<unsigned long long*>(acc + 4);
   DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, 256, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(acc, 0, 64, s));
-  auto orth = [&](double* Zp, int rows) -> int {
-    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, err, s);
+  auto orth = [&](double* Zp, int rows, bool exact) -> int {
+    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, err, exact, s);
   };
 
   // canonical problem: keep the left basis of Th (M x N)
@@ -443,10 +305,10 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   for (int it = 0; it < iters; ++it) {
     // Y = Th^T S (N x k), W = orth(Y)
     DMRG_TRY(tf32x3_gemm_ex(1, 0, N, k, M, 1.f, Th, N, S, k, 0, Y, k, gw, err, s));
-    DMRG_TRY(orth(Y, N));
+    DMRG_TRY(orth(Y, N, false));
     // Z = Th W (M x k), Q = orth(Z)  (into S)
     DMRG_TRY(tf32x3_gemm_ex(0, 0, M, k, N, 1.f, Th, N, Y, k, 0, S, k, gw, err, s));
-    DMRG_TRY(orth(S, M));
+    DMRG_TRY(orth(S, M, it == iters - 1));
   }
   // C = Q^T Th (k x N)
   DMRG_TRY(tf32x3_gemm_ex(1, 0, k, N, M, 1.f, S, k, Th, N, 0, C, N, gw, err, s));

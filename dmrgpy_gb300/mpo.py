@@ -65,14 +65,19 @@ def _site_matrices(ops, types):
     return mats
 
 
-def compile_terms(types, terms):
-    """-> (list of (coef, first_site, [matrices over the span]), is_real).
-    Sites are 0-based here."""
+def compile_terms(types, terms, keep_zero=False):
+    """-> (list of (coef, first_site, [matrices over the span], factor,
+    term index), is_real).  Sites are 0-based here.  `factor` is the compiled
+    coefficient per unit input coefficient (reordering sign times the powers
+    of i moved out of imaginary site operators), so coef = factor * input
+    coefficient.  Zero-coefficient terms are dropped unless keep_zero."""
     out = []
     real = True
-    for coef, factors in terms:
-        c, ops = _order_and_sign(coef, factors)
-        if c == 0:
+    for t, (coef, factors) in enumerate(terms):
+        c, ops = _order_and_sign(1.0, factors)
+        factor = c
+        c = c * complex(coef)
+        if c == 0 and not keep_zero:
             continue
         mats = _site_matrices(ops, types)
         nontriv = [i for i, m in enumerate(mats) if not np.allclose(m, np.eye(m.shape[0]), atol=0.0, rtol=0.0)]
@@ -87,12 +92,13 @@ def compile_terms(types, terms):
                 span.append(m.real.copy())
             elif np.all(m.real == 0):
                 c = c * 1j
+                factor = factor * 1j
                 span.append((m / 1j).real.copy())
             else:
                 span.append(m)
                 real = False
-        out.append((c, f, span))
-    for c, _, _ in out:
+        out.append((c, f, span, factor, t))
+    for c, _, _, _, _ in out:
         if abs(c.imag) > 1e-15 * max(1.0, abs(c)):
             real = False
     return out, real
@@ -111,12 +117,19 @@ class _OpTable:
         return self.ids[k]
 
 
-def build_mpo(types, terms, compress_above=16, cutoff=1e-14):
+def build_mpo(types, terms, compress_above=16, cutoff=1e-14, coupling_map=False):
     """Compile `terms` on sites of type codes `types` into a list of MPO
-    tensors (w_left, d, d, w_right); returns (W, is_real)."""
+    tensors (w_left, d, d, w_right); returns (W, is_real).
+
+    With coupling_map=True the automaton keeps zero-coefficient terms, is
+    never compressed, and (W, is_real, cmap) is returned: cmap[t] =
+    (site, ls, rs, M, factor) says that term t contributes
+    factor * coef_t * M (stored (d_in, d_out)) to W[site][ls, :, :, rs], so W
+    is affine in the coefficients and dW/dcoef_t is that single block."""
     n = len(types)
     dims = [S.dim(c) for c in types]
-    compiled, real = compile_terms(types, terms)
+    compiled, real = compile_terms(types, terms, keep_zero=coupling_map)
+    cmap = [None] * len(terms)
     dtype = np.float64 if real else np.complex128
     table = _OpTable()
     # states per bond b (between sites b-1 and b, b = 0..n): dict key -> index
@@ -136,11 +149,12 @@ def build_mpo(types, terms, compress_above=16, cutoff=1e-14):
         else:
             entries[site][key] = mat.astype(dtype if real else complex)
 
-    for c, f, span in compiled:
+    for c, f, span, factor, t in compiled:
         cval = c.real if real else c
         l = f + len(span) - 1
         if l == f:
             add(f, bond_states[f][START], bond_states[f + 1][DONE], cval * span[0])
+            cmap[t] = (f, bond_states[f][START], bond_states[f + 1][DONE], span[0].T.copy(), factor)
             continue
         prefix = ()
         prev = bond_states[f][START]
@@ -154,6 +168,7 @@ def build_mpo(types, terms, compress_above=16, cutoff=1e-14):
                 add(site, prev, states[skey], m)
             prev = states[skey]
         add(l, prev, bond_states[l + 1][DONE], cval * span[-1])
+        cmap[t] = (l, prev, bond_states[l + 1][DONE], span[-1].T.copy(), factor)
 
     W = []
     for i in range(n):
@@ -167,7 +182,8 @@ def build_mpo(types, terms, compress_above=16, cutoff=1e-14):
         for (ls, rs), m in entries[i].items():
             T[ls, :, :, rs] += m.T  # textbook (out,in) -> stored (in,out)
         W.append(T)
-    # the first/last tensors keep only the start / done rows
+    if coupling_map:
+        return W, real, cmap
     if max(w.shape[3] for w in W) > compress_above:
         W = compress(W, cutoff)
     return W, real

@@ -113,6 +113,18 @@ int dmrg_env_extend_right(int dtype, int precision, int chil, int d, int chir, i
                           const void* R, const void* W, const void* B, void* Rnew,
                           void* work, size_t work_bytes, void* stream);
 
+/* ---- adjoint of the environment chain (FP64) ----------------------------- */
+size_t dmrg_env_gradient_workspace_bytes(int dtype, int chil, int d, int chir, int wl, int wr);
+/* G (wl, d, d, wr) = d<psi|H|psi>/dW_i = L (chil, wl, chil) . A . conj(A) .
+ * R (chir, wr, chir) with A (chil, d, chir) the site tensor, L/R the
+ * environments of the sites left/right of it.  No reference function: the
+ * reference has no derivative features; the result is checked against
+ * finite differences of its energies and against <dH/dlambda> evaluated with
+ * its expectation value (pyitensor/chain.py:277-287). */
+int dmrg_env_gradient(int dtype, int chil, int d, int chir, int wl, int wr,
+                      const void* L, const void* A, const void* R, void* G,
+                      void* work, size_t work_bytes, void* stream);
+
 /* ---- Krylov solvers ------------------------------------------------------ */
 size_t dmrg_lanczos_workspace_bytes(const dmrg_heff_t* op, int niter);
 /* Lowest eigenpair of H_eff by Lanczos with full reorthogonalisation; stops
