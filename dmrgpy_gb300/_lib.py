@@ -19,6 +19,10 @@ DMRG_ERR_NOCONV = 5
 DMRG_ERR_TIMEOUT = 6
 DMRG_ERR_UNSUPPORTED = 7
 
+# size of the fixed device array behind dmrg_heff_apply_noalloc
+# (DMRG_NOALLOC_SCRATCH_BYTES in include/dmrg_gb300.h)
+NOALLOC_SCRATCH_BYTES = 64 << 20
+
 REAL64 = 0
 COMPLEX128 = 1
 PREC_FP64 = 0
@@ -51,6 +55,7 @@ SIGNATURES = [
     ("dmrg_heff_apply_prepared", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_void_p, c_void_p, c_size_t,
                                          c_void_p]),
     ("dmrg_heff_status", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_size_t, c_void_p]),
+    ("dmrg_heff_apply_noalloc", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_void_p, c_void_p]),
     ("dmrg_env_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     ("dmrg_env_extend_left", c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                      c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),

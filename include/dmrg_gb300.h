@@ -99,6 +99,22 @@ int dmrg_heff_apply_prepared(const dmrg_heff_t* op, const void* x, void* y,
                              void* work, size_t work_bytes, void* stream);
 int dmrg_heff_status(const dmrg_heff_t* op, void* work, size_t work_bytes, void* stream);
 
+/* Allocation-free FP64 matvec: y = H_eff x like dmrg_heff_apply, with the
+ * scratch taken from one fixed device array inside the library instead of a
+ * caller workspace; the call allocates nothing.  It has no counterpart in the
+ * reference (whose matvec allocates its NumPy intermediates on every call).
+ * For callers that cannot allocate device memory per call (no device
+ * allocator of their own, or a memory budget fixed at start-up).
+ * precision must be DMRG_PREC_FP64 (else DMRG_ERR_UNSUPPORTED); an operator
+ * whose dmrg_heff_workspace_bytes() exceeds DMRG_NOALLOC_SCRATCH_BYTES is
+ * rejected with DMRG_ERR_WORKSPACE.  The first call on a device sets up the
+ * array's address and should come before any stream capture.  All calls share
+ * the array: calls that may execute at the same time race and must be
+ * serialised by the caller (e.g. one stream); nothing in it needs to start
+ * at zero. */
+#define DMRG_NOALLOC_SCRATCH_BYTES (64u << 20)
+int dmrg_heff_apply_noalloc(const dmrg_heff_t* op, const void* x, void* y, void* stream);
+
 /* ---- environments ----------------------------------------------------- */
 size_t dmrg_env_workspace_bytes(int dtype, int precision, int chil, int d, int chir, int wl, int wr);
 /* Lnew (chir, wr, chir) = L (chil, wl, chil) . conj(A) . W . A with
