@@ -79,6 +79,7 @@ class Chain:
 
     def set_hamiltonian(self, terms):
         self.H = self.build_operator(terms)
+        self.H_terms = list(terms)
         self.have_H = True
         self._wf0_energy = None
 
@@ -121,6 +122,22 @@ class Chain:
         self._wf0_energy = energy
         self.last_stats = eng.stats
         return energy
+
+    def gs_energy_gradient(self):
+        """dE/dc_t for every term t of the Hamiltonian (as given to
+        set_hamiltonian) at the current ground state, from one adjoint pass
+        over the environments (:mod:`dmrgpy_gb300.gradients`).  Runs
+        gs_energy first if needed.  Returns a complex NumPy array; for a
+        Hermitian pair of terms with a real coupling the sum is real."""
+        from .gradients import CouplingProblem
+        if not self.have_H:
+            raise RuntimeError("Chain.gs_energy_gradient called before set_hamiltonian")
+        if self.wf0 is None or self._wf0_energy is None:
+            self.gs_energy()
+        prob = CouplingProblem(self.site_types, self.H_terms)
+        A = prob.engine.to_device(self.wf0.tensors)
+        _, grad = prob.gradient(A)
+        return grad
 
     def gs_wavefunction(self):
         if self.wf0 is None:

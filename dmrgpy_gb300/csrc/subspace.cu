@@ -178,8 +178,47 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
   atomicMax(dev, __double_as_longlong(mx));
 }
 
+// The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
+// what a product accurate to ~5e-7 can resolve.  A left basis that is only
+// that orthonormal makes the norm environment drift by ~N x 1e-6 over a
+// chain, so a kept basis gets one correction with an FP64 Gram:
+//   E = X^T X - I (FP64),  X <- X (I - E/2)   (residual O(E^2)),
+// where the product X (E/2) only needs the split-TF32 relative accuracy
+// because E is already tiny.
+int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* B, unsigned long long* dev, void* gw,
+                      int* err, cudaStream_t s) {
+  TGemm g{};
+  g.B = ax(1); g.M = ax(k); g.K = ax(m); g.N = ax(k);
+  g.a_m = st(1); g.a_k = st(ld);
+  g.b_k = st(ld); g.b_n = st(1);
+  g.c_m = st(k); g.c_n = st(1);
+  DMRG_TRY(tgemm<double>(g, 1.0, Z, Z, 0.0, A, s));
+  DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+  poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
+  DMRG_CHECK_LAUNCH();
+  return tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s);
+}
+
+// max|A - I| of a k x k Gram matrix (host value; synchronises the stream)
+int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, double* out, cudaStream_t s) {
+  DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+  poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
+  DMRG_CHECK_LAUNCH();
+  unsigned long long h = 0;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  memcpy(out, &h, sizeof(double));
+  return DMRG_OK;
+}
+
 int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
                unsigned long long* dev, void* gw, int* err, bool exact, cudaStream_t s) {
+  // an input that is already orthonormal (the usual warm start) skips the
+  // iterations
+  double d0 = 1.0;
+  DMRG_TRY(tf32x3_gemm_ex(1, 0, k, k, m, 1.f, Z, ld, Z, ld, 0, A, k, gw, err, s));
+  DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
+  if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, err, s) : DMRG_OK;
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
   colsq_kernel<<<(k + 255) / 256, 256, 0, s>>>(Z, ld, m, k, n2);
   DMRG_CHECK_LAUNCH();
@@ -221,25 +260,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
     Y = t;
   }
   if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
-  if (exact) {
-    // The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
-    // what a product accurate to ~5e-7 can resolve.  A left basis that is
-    // only that orthonormal makes the norm environment drift by ~N x 1e-6
-    // over a chain, so the kept basis gets one correction with an FP64 Gram:
-    //   E = X^T X - I (FP64),  X <- X (I - E/2)   (residual O(E^2)),
-    // where the product X (E/2) only needs the split-TF32 relative accuracy
-    // because E is already tiny.
-    TGemm g{};
-    g.B = ax(1); g.M = ax(k); g.K = ax(m); g.N = ax(k);
-    g.a_m = st(1); g.a_k = st(ld);
-    g.b_k = st(ld); g.b_n = st(1);
-    g.c_m = st(k); g.c_n = st(1);
-    DMRG_TRY(tgemm<double>(g, 1.0, Z, Z, 0.0, A, s));
-    DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-    poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
-    DMRG_CHECK_LAUNCH();
-    DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s));
-  }
+  if (exact) DMRG_TRY(orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, err, s));
   return DMRG_OK;
 }
 
@@ -254,9 +275,18 @@ size_t subspace_workspace_bytes(int m, int n, int k) {
 }
 
 // theta (m x n row-major).  absorb 0 keeps an orthonormal LEFT basis; X is
-// the start basis m x kx (ld kx).  absorb 1 keeps an orthonormal RIGHT basis;
-// X is kx x n (ld n).  k vectors are kept; start columns beyond kx are random.
+// the tensor on the other side of the bond, kx x n (ld n) with (nominally)
+// orthonormal rows.  absorb 1 keeps an orthonormal RIGHT basis; X is the
+// left tensor, m x kx (ld kx) with orthonormal columns.  k vectors are kept;
+// start vectors beyond kx are random.
 // Outputs: left (m x k), right (k x n), *disc = discarded weight fraction.
+//
+// The start is an orthonormal basis of the OTHER side (the right space for
+// a kept left basis) because it is exactly orthonormal in a canonical MPS,
+// whereas the centre tensor on the kept side carries the singular values:
+// starting from it, its weak directions sit ~s_k^2/s_1^2 below the strong
+// ones after the first product and drown in the FP32-level rounding of the
+// orthonormalisation.
 int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,
                       double* left, double* right, double* disc, void* work, size_t work_bytes, cudaStream_t s) {
   if (k <= 0 || k > m || k > n || kx < 0 || kx > k || iters < 1 || iters > 8) return DMRG_ERR_ARG;
@@ -269,7 +299,6 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   double* S = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* Y = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* C = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
-  double* Xs = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* PX = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* PA = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* PB_ = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
@@ -283,32 +312,34 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
     return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, err, exact, s);
   };
 
-  // canonical problem: keep the left basis of Th (M x N)
+  // canonical problem: keep the left basis of Th (M x N); W (N x k) is an
+  // orthonormal basis of the other side
   const double* Th = theta;
   int M = m, N = n;
-  const double* Xc = X;
-  long long ldx = kx;
   if (absorb == 1) {
     DMRG_TRY(transpose(theta, n, m, n, Tt, m, s));   // Tt = theta^T (n x m)
     Th = Tt; M = n; N = m;
-    if (kx > 0) DMRG_TRY(transpose(X, n, kx, n, Xs, kx, s));  // Xs = X^T (n x kx)
-    Xc = Xs;
-  }
-  if (kx > 0) {
-    copy2d_kernel<<<egrid((long long)M * kx), 256, 0, s>>>(Xc, ldx, S, k, M, kx);
-    DMRG_CHECK_LAUNCH();
+    if (kx > 0) {
+      copy2d_kernel<<<egrid((long long)N * kx), 256, 0, s>>>(X, kx, Y, k, N, kx);   // W0 = X (m x kx)
+      DMRG_CHECK_LAUNCH();
+    }
+  } else if (kx > 0) {
+    DMRG_TRY(transpose(X, n, kx, n, Y, k, s));       // W0 = X^T (n x kx)
   }
   if (kx < k) {
-    random_fill_kernel<<<egrid((long long)M * (k - kx)), 256, 0, s>>>(S, k, M, kx, k, 0x51ab5eedULL + (unsigned)M);
+    random_fill_kernel<<<egrid((long long)N * (k - kx)), 256, 0, s>>>(Y, k, N, kx, k, 0x51ab5eedULL + (unsigned)N);
     DMRG_CHECK_LAUNCH();
   }
+  DMRG_TRY(orth(Y, N, false));
   for (int it = 0; it < iters; ++it) {
-    // Y = Th^T S (N x k), W = orth(Y)
-    DMRG_TRY(tf32x3_gemm_ex(1, 0, N, k, M, 1.f, Th, N, S, k, 0, Y, k, gw, err, s));
-    DMRG_TRY(orth(Y, N, false));
-    // Z = Th W (M x k), Q = orth(Z)  (into S)
+    // Z = Th W (M x k), Q = orth(Z) (into S)
     DMRG_TRY(tf32x3_gemm_ex(0, 0, M, k, N, 1.f, Th, N, Y, k, 0, S, k, gw, err, s));
     DMRG_TRY(orth(S, M, it == iters - 1));
+    if (it + 1 < iters) {
+      // W = orth(Th^T Q) (N x k)
+      DMRG_TRY(tf32x3_gemm_ex(1, 0, N, k, M, 1.f, Th, N, S, k, 0, Y, k, gw, err, s));
+      DMRG_TRY(orth(Y, N, false));
+    }
   }
   // C = Q^T Th (k x N)
   DMRG_TRY(tf32x3_gemm_ex(1, 0, k, N, M, 1.f, S, k, Th, N, 0, C, N, gw, err, s));

@@ -362,14 +362,17 @@ class Engine:
         m, n = cl * d1, d2 * cr
         if self.use_subspace(m, n, cutoff, maxdim):
             rank = min(maxdim, m, n)
+            # warm start: the orthonormal tensor on the other side of the bond
+            # (right-canonical A_j in a left-to-right pass, left-canonical A_i
+            # in a right-to-left pass)
             if absorb == 0:
-                start = Ai.reshape(m, Ai.shape[2])
-                kx = min(start.shape[1], rank)
-                start = start[:, :kx].contiguous()
-            else:
                 start = Aj.reshape(Aj.shape[0], n)
                 kx = min(start.shape[0], rank)
                 start = start[:kx].contiguous()
+            else:
+                start = Ai.reshape(m, Ai.shape[2])
+                kx = min(start.shape[1], rank)
+                start = start[:, :kx].contiguous()
             lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb)
         else:
             lo, ro, s, keep, disc = self.svd(theta.view(m, n), cutoff, maxdim, 1, absorb)

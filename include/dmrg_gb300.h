@@ -184,15 +184,19 @@ int dmrg_svd_truncate(int dtype, int m, int n, const void* M,
                       void* work, size_t work_bytes, void* stream);
 
 /* Fixed-rank truncation for the split-TF32 sweep when maxdim binds
- * (cutoff <= 0): keeps k = maxdim vectors found by one warm-started
- * subspace iteration with block Gram-Schmidt orthonormalisation (all
- * contractions split-TF32 on tcgen05), instead of a full SVD.  Real dtype.
+ * (cutoff <= 0): keeps k = maxdim vectors found by warm-started subspace
+ * iteration with polar (Newton-Schulz) orthonormalisation (all contractions
+ * split-TF32 on tcgen05) and an FP64-Gram correction of the kept basis,
+ * instead of a full SVD.  Real dtype.
  *   absorb 0: left_out (m x k) orthonormal columns, right_out = left^T theta
- *             (k x n); start = current left tensor as m x kstart (ld kstart)
+ *             (k x n); start = the current RIGHT tensor as kstart x n
+ *             (orthonormal rows in a right-canonical MPS)
  *   absorb 1: right_out (k x n) orthonormal rows, left_out = theta right^T
- *             (m x k); start = current right tensor as kstart x n
- * Start vectors beyond kstart are random; iters (1..8) subspace iterations
- * are run.  *discarded receives the weight of
+ *             (m x k); start = the current LEFT tensor as m x kstart
+ *             (ld kstart, orthonormal columns in a left-canonical MPS)
+ * A start that is not orthonormal is orthonormalised first; start vectors
+ * beyond kstart are random.  iters (1..8): products with theta per side
+ * (1 = kept basis from theta . start).  *discarded receives the weight of
  * theta outside the kept space over |theta|^2.  Stands in for the
  * maxdim-bound case of pyitensor/svd.py:154-195 as used by
  * pyitensor/dmrg.py:336-352 (singular values are not formed). */

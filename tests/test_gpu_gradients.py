@@ -103,3 +103,19 @@ def test_field_gradient_matches_finite_differences_and_autograd():
     E.backward()
     assert abs(E.item() - _ed(types, terms_of(h))[0]) / n < 1e-10
     assert abs(hh.grad.item() - dedh) < 1e-12 * max(1.0, abs(dedh))
+
+
+def test_chain_session_gradient():
+    from dmrgpy_gb300.chain import Chain
+    n = 8
+    terms = terms_tfim(n, 1.0, 1.1)
+    ch = Chain([2] * n)
+    ch.set_sweep_params(16, 8, 1e-14, 0.0)
+    ch.set_hamiltonian(terms)
+    np.random.seed(4)
+    g = ch.gs_energy_gradient()
+    e0, v0 = _ed([2] * n, terms)
+    assert abs(ch.gs_energy(skip_dmrg=True) - e0) / n < 1e-10
+    for t, (c, f) in enumerate(terms):
+        ht = O.dense_hamiltonian([2] * n, [(1.0 + 0j, f)])
+        assert abs(g[t] - np.vdot(v0, ht @ v0)) < 1e-6
