@@ -34,6 +34,7 @@ c_double = ctypes.c_double
 c_void_p = ctypes.c_void_p
 P_int = ctypes.POINTER(ctypes.c_int)
 P_double = ctypes.POINTER(ctypes.c_double)
+P_void = ctypes.POINTER(ctypes.c_void_p)
 
 
 class HeffDesc(ctypes.Structure):
@@ -79,6 +80,20 @@ SIGNATURES = [
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    ("dmrg_batch_gemm_workspace_bytes", c_size_t, [c_int]),
+    ("dmrg_batch_gemm", c_int, [c_int, c_int, P_int, P_int, P_int, P_void, P_void, P_void, c_void_p, c_size_t,
+                                c_void_p]),
+    ("dmrg_batch_env_workspace_bytes", c_size_t, [c_int, c_int, c_int, P_int, P_int, P_int, P_int, P_int]),
+    ("dmrg_batch_env_extend", c_int, [c_int, c_int, c_int, P_int, P_int, P_int, P_int, P_int, P_void, P_void,
+                                      P_void, P_void, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_batch_lanczos_workspace_bytes", c_size_t, [c_int, ctypes.POINTER(HeffDesc), c_int]),
+    ("dmrg_batch_lanczos_ground", c_int, [c_int, ctypes.POINTER(HeffDesc), P_void, c_int, c_double, c_int, P_double,
+                                          P_int, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_batch_svd_workspace_bytes", c_size_t, [c_int, c_int, P_int, P_int]),
+    ("dmrg_batch_svd_factor", c_int, [c_int, c_int, P_int, P_int, P_void, c_double, P_int, c_int, c_int, P_int,
+                                      P_double, P_double, c_int, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_batch_svd_output", c_int, [c_int, c_int, P_int, P_int, P_int, c_int, P_void, P_void, c_void_p, c_size_t,
+                                      c_void_p]),
 ]
 
 

@@ -16,6 +16,8 @@ namespace dmrg {
 
 static std::atomic<unsigned long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void uncount_launches(unsigned long long n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 namespace {
 
@@ -76,6 +78,8 @@ int heff_run(const dmrg_heff_t* o, const T* x, T* y, void* work, cudaStream_t s)
   T* Qp = reinterpret_cast<T*>(static_cast<char*>(work) + align_up(P * sizeof(T)));
   return heff_apply_fp64<T>(*o, x, y, Pp, Qp, s);
 }
+
+}  // namespace
 
 // ---- symmetric tridiagonal eigenproblem (implicit QL with Wilkinson-type
 // shifts, Golub & Van Loan sec. 8.3 / the EISPACK tql2 scheme).  d: diagonal
@@ -157,6 +161,8 @@ int lowest_ritz(const std::vector<double>& al, const std::vector<double>& be, do
   }
   return DMRG_OK;
 }
+
+namespace {
 
 
 // ---- workspace layout of the Krylov drivers
@@ -356,6 +362,8 @@ int expm_impl(const dmrg_heff_t* o, T* x, std::complex<double> coeff, int niter,
   return DMRG_ERR_ARG;  // unreachable: the it == m-1 branch returns
 }
 
+}  // namespace
+
 // cutoff/maxdim/mindim rule of pyitensor/svd.py:32-68 on descending s
 void keep_rule(const double* s, int n, double cutoff, int maxdim, int mindim, int* keep, double* disc) {
   std::vector<double> p(n);
@@ -394,6 +402,8 @@ void keep_rule(const double* s, int n, double cutoff, int maxdim, int mindim, in
   for (int i = *keep; i < n; ++i) d += p[i];
   *disc = d;
 }
+
+namespace {
 
 template <typename T>
 int svd_impl(int m, int n, const T* M, double cutoff, int maxdim, int mindim, int absorb, T* lo, T* ro, double* svals,

@@ -65,6 +65,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // Every kernel launch of the library is followed by this check, which also
 // counts the launch (dmrg_kernel_launches()).
 void count_launch();
+void count_launches(unsigned long long n);    // kernels of a replayed graph
+void uncount_launches(unsigned long long n);  // launches made during a graph capture
 #define DMRG_CHECK_LAUNCH()                                      \
   do {                                                           \
     cudaError_t _e = cudaGetLastError();                         \
@@ -130,6 +132,19 @@ inline St2 st(long long s1, long long s2 = 0) { St2 s; s.s1 = s1; s.s2 = s2; ret
 
 template <typename T>
 int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStream_t stream);
+// Many strided contractions of different shapes in one launch.  desc_host
+// (pageable, tgemm_grouped_desc_bytes(nprob)) stages the problem table that
+// is copied to desc_dev (device, same size) on the stream.
+size_t tgemm_grouped_desc_bytes(int nprob);
+// the same split in two: the problem table built on the host (desc_host),
+// then -- after the caller has copied it to device memory -- the launch
+int tgemm_grouped_build(int nprob, const TGemm* g, const void* const* A, const void* const* B, void* const* C,
+                        void* desc_host, int* nout, long long* tiles_out);
+template <typename T>
+int tgemm_grouped_launch(const void* desc_dev, int n, long long tiles, T alpha, T beta, cudaStream_t stream);
+template <typename T>
+int tgemm_grouped(int nprob, const TGemm* g, const void* const* A, const void* const* B, void* const* C, T alpha,
+                  T beta, void* desc_dev, void* desc_host, cudaStream_t stream);
 
 // ---------------------------------------------------------------- vector ops (device scalars)
 template <typename T> int vdot(const T* x, const T* y, long long n, T* out, double* scratch, cudaStream_t s);

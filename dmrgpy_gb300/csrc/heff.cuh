@@ -1,10 +1,26 @@
 // Internal interface of the H_eff / environment contraction plans.
 #pragma once
+#include <vector>
+
 #include "common.cuh"
 
 namespace dmrg {
 
 // FP64 / complex FP64 path (strided CUDA-core contractions)
+// one strided contraction of a plan (alpha 1, beta 0)
+struct GStep {
+  TGemm g;
+  const void* A;
+  const void* B;
+  void* C;
+};
+template <typename T> int heff_fp64_plan(const dmrg_heff_t& o, const T* x, T* y, T* P, T* Q, GStep* steps);
+template <typename T>
+int env_left_plan(long long cl, long long d, long long cr, long long wl, long long wr, const T* L, const T* W,
+                  const T* A, T* Lnew, T* P, GStep* steps);
+template <typename T>
+int env_right_plan(long long cl, long long d, long long cr, long long wl, long long wr, const T* R, const T* W,
+                   const T* B, T* Rnew, T* P, GStep* steps);
 template <typename T> size_t heff_fp64_elems(const dmrg_heff_t& o, size_t* p_elems, size_t* q_elems);
 template <typename T> int heff_apply_fp64(const dmrg_heff_t& o, const T* x, T* y, T* P, T* Q, cudaStream_t s);
 size_t env_fp64_elems(int side, long long cl, long long d, long long cr, long long wl, long long wr);
@@ -19,6 +35,20 @@ int env_right_fp64(long long cl, long long d, long long cr, long long wl, long l
 size_t svd_work_bytes(int dtype, int m, int n);
 template <typename T> int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, int abs_floor, cudaStream_t s);
 template <typename T> int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s);
+
+// batched truncated SVD (one CTA per problem)
+size_t svd_batch_work_bytes(int dtype, int nprob, const int* m, const int* n);
+template <typename T>
+int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const* M, void* work, double* host_s,
+                          int ld_s, int abs_floor, cudaStream_t s);
+template <typename T>
+int hestenes_batch_output(int nprob, const int* m, const int* n, const int* keep, int absorb, void* work,
+                          T* const* lo, T* const* ro, cudaStream_t s);
+
+// host-side pieces of the Krylov drivers and of the truncation rule
+bool tridiag_eig(int n, std::vector<double>& d, std::vector<double> e, std::vector<double>* z);
+int lowest_ritz(const std::vector<double>& al, const std::vector<double>& be, double* ev, std::vector<double>* vec);
+void keep_rule(const double* s, int n, double cutoff, int maxdim, int mindim, int* keep, double* disc);
 
 // vector ops
 template <typename T> int vaxpy2(T* y, const T* x1, const double* a1, const T* x2, const double* a2, long long n, cudaStream_t s);

@@ -13,6 +13,8 @@
 // are the column norms of X; the singular vectors are X/sigma and V.  Unlike
 // the Gram-matrix route this keeps small singular values to high relative
 // accuracy, so no exact-SVD fallback is needed.
+#include <vector>
+
 #include "common.cuh"
 
 namespace dmrg {
@@ -278,6 +280,165 @@ __global__ void out_kernel(const T* __restrict__ X, const T* __restrict__ V, con
   }
 }
 
+// ---------------------------------------------------------------- batched
+// Many small SVDs at once (one CTA per problem, X and V in global memory):
+// the same one-sided Jacobi with the same tolerances as the single-problem
+// kernel, rounds separated by __syncthreads().  Used by the batched sweep of
+// many independent chains.
+template <typename T>
+struct BSvd {
+  const T* M;
+  int m, n, left, r, c;
+  T* X;
+  T* V;
+  double* sig;
+  double* sorted;
+  int* perm;
+  int* info;  // [0] sweeps (negative: sweep limit reached)
+  int abs_floor;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(1024) hestenes_batch_kernel(const BSvd<T>* __restrict__ tab, int max_sweeps) {
+  const BSvd<T> a = tab[blockIdx.x];
+  __shared__ double red[32];
+  __shared__ unsigned rot;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int r = a.r, c = a.c, cp = c + (c & 1), half = cp / 2;
+  T* X = a.X;
+  T* V = a.V;
+  const long long mn = (long long)a.m * a.n;
+  double part = 0.0;
+  for (long long idx = threadIdx.x; idx < mn; idx += blockDim.x) {
+    T v;
+    if (a.left) {
+      v = Sc<T>::conj(a.M[idx]);
+    } else {
+      const int j = (int)(idx / a.m), i = (int)(idx - (long long)j * a.m);
+      v = a.M[(long long)i * a.n + j];
+    }
+    X[idx] = v;
+    part += Sc<T>::abs2(v);
+  }
+  for (long long idx = threadIdx.x; idx < (long long)c * c; idx += blockDim.x) {
+    const int col = (int)(idx / c), row = (int)(idx - (long long)col * c);
+    V[idx] = row == col ? Sc<T>::one() : Sc<T>::zero();
+  }
+  part = warp_sum(part);
+  if (lane == 0) red[wid] = part;
+  __syncthreads();
+  double fro2 = 0.0;
+  for (int w = 0; w < nw; ++w) fro2 += red[w];
+  const double abs_floor = a.abs_floor ? 1e-16 * fro2 : 0.0;
+  double tol = 2.2e-16 * sqrt((double)r);
+  tol = tol > 1e-15 ? tol : 1e-15;
+  int sweep = 0;
+  bool converged = cp < 2;
+  for (; sweep < max_sweeps && !converged; ++sweep) {
+    if (threadIdx.x == 0) rot = 0u;
+    __syncthreads();
+    for (int round = 0; round < cp - 1; ++round) {
+      for (int i = wid; i < half; i += nw) {
+        int p = player(i, round, cp), q = player(cp - 1 - i, round, cp);
+        if (p > q) { const int t = p; p = q; q = t; }
+        if (q >= c) continue;
+        T* xp = X + (long long)p * r;
+        T* xq = X + (long long)q * r;
+        double al, be, gre, gim;
+        gram2<T>(xp, xq, r, lane, al, be, gre, gim);
+        al = warp_sum(al);
+        be = warp_sum(be);
+        gre = warp_sum(gre);
+        gim = warp_sum(gim);
+        const double ag = sqrt(gre * gre + gim * gim);
+        const double scale = sqrt(al) * sqrt(be);
+        if (!(ag > tol * scale) || !(ag > abs_floor) || !(ag > 1e-300)) continue;
+        const double tau = (be - al) / (2.0 * ag);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        const double cs = 1.0 / sqrt(1.0 + t * t);
+        const double sn = t * cs;
+        const T e = Sc<T>::make(gre / ag, gim / ag);
+        rot_cols<T>(xp, xq, r, lane, cs, sn, e);
+        rot_cols<T>(V + (long long)p * c, V + (long long)q * c, c, lane, cs, sn, e);
+        if (lane == 0) atomicAdd(&rot, 1u);
+      }
+      __syncthreads();
+    }
+    converged = (*(volatile unsigned*)&rot == 0u);
+    __syncthreads();
+  }
+  // singular values, then their descending (stable) order
+  for (int col = wid; col < c; col += nw) {
+    const T* x = X + (long long)col * r;
+    double s2 = 0.0;
+    for (int i = lane; i < r; i += 32) s2 += Sc<T>::abs2(x[i]);
+    s2 = warp_sum(s2);
+    if (lane == 0) a.sig[col] = sqrt(s2);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < c; i += blockDim.x) {
+    const double v = a.sig[i];
+    int rank = 0;
+    for (int j = 0; j < c; ++j) {
+      const double u = a.sig[j];
+      rank += (u > v) || (u == v && j < i);
+    }
+    a.perm[rank] = i;
+    a.sorted[rank] = v;
+  }
+  if (threadIdx.x == 0) a.info[0] = converged ? sweep : -sweep;
+}
+
+template <typename T>
+struct BOut {
+  const T* X;
+  const T* V;
+  const int* perm;
+  const double* sorted;
+  int m, n, left, keep;
+  T* lo;
+  T* ro;
+};
+
+// grid (blocks, nprob): the single-problem out_kernel per problem
+template <typename T>
+__global__ void out_batch_kernel(const BOut<T>* __restrict__ tab, int absorb) {
+  const BOut<T> o = tab[blockIdx.y];
+  const int m = o.m, n = o.n, keep = o.keep;
+  const long long nl = (long long)m * keep, nr = (long long)keep * n;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < nl + nr; idx += stride) {
+    if (idx < nl) {
+      const int i = (int)(idx / keep), k = (int)(idx - (long long)i * keep);
+      const int pk = o.perm[k];
+      const double sg = o.sorted[k];
+      T v;
+      if (o.left) {
+        v = o.V[(long long)pk * m + i];
+        if (absorb == 1) v = Sc<T>::scale(v, sg);
+      } else {
+        v = o.X[(long long)pk * m + i];
+        if (absorb != 1) v = Sc<T>::scale(v, sg > 0.0 ? 1.0 / sg : 0.0);
+      }
+      o.lo[idx] = v;
+    } else {
+      const long long q = idx - nl;
+      const int k = (int)(q / n), j = (int)(q - (long long)k * n);
+      const int pk = o.perm[k];
+      const double sg = o.sorted[k];
+      T v;
+      if (o.left) {
+        v = Sc<T>::conj(o.X[(long long)pk * n + j]);
+        if (absorb != 0) v = Sc<T>::scale(v, sg > 0.0 ? 1.0 / sg : 0.0);
+      } else {
+        v = Sc<T>::conj(o.V[(long long)pk * n + j]);
+        if (absorb == 0) v = Sc<T>::scale(v, sg);
+      }
+      o.ro[q] = v;
+    }
+  }
+}
+
 inline int egrid(long long n) {
   long long g = (n + 255) / 256;
   if (g > 152 * 8) g = 152 * 8;
@@ -419,6 +580,128 @@ int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }
+
+// ---- batched host drivers
+namespace {
+struct BLayout {
+  size_t total;
+  std::vector<size_t> X, V, sig, sorted, perm, info;
+  size_t tab, otab;
+};
+
+BLayout batch_layout(size_t es, int nprob, const int* m, const int* n, size_t tab_es, size_t otab_es) {
+  BLayout L;
+  size_t off = 0;
+  L.tab = off; off += align_up(tab_es * (size_t)nprob);
+  L.otab = off; off += align_up(otab_es * (size_t)nprob);
+  L.X.resize(nprob); L.V.resize(nprob); L.sig.resize(nprob); L.sorted.resize(nprob); L.perm.resize(nprob);
+  L.info.resize(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    const size_t c = (size_t)(m[p] < n[p] ? m[p] : n[p]);
+    const size_t r = (size_t)(m[p] < n[p] ? n[p] : m[p]);
+    L.X[p] = off; off += align_up(r * c * es);
+    L.V[p] = off; off += align_up(c * c * es);
+    L.sig[p] = off; off += align_up(c * 8);
+    L.sorted[p] = off; off += align_up(c * 8);
+    L.perm[p] = off; off += align_up(c * 4);
+    L.info[p] = off; off += align_up(8);
+  }
+  L.total = off;
+  return L;
+}
+}  // namespace
+
+size_t svd_batch_work_bytes(int dtype, int nprob, const int* m, const int* n) {
+  const size_t es = dtype == DMRG_COMPLEX128 ? 16 : 8;
+  return batch_layout(es, nprob, m, n, sizeof(BSvd<cplx>), sizeof(BOut<cplx>)).total;
+}
+
+// Phase 1 for every problem; the sorted singular values of problem p go to
+// host_s + p * ld_s.
+template <typename T>
+int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const* M, void* work, double* host_s,
+                          int ld_s, int abs_floor, cudaStream_t s) {
+  const BLayout L = batch_layout(sizeof(T), nprob, m, n, sizeof(BSvd<cplx>), sizeof(BOut<cplx>));
+  char* base = static_cast<char*>(work);
+  std::vector<BSvd<T>> tab(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    BSvd<T>& a = tab[p];
+    a.M = M[p];
+    a.m = m[p];
+    a.n = n[p];
+    a.left = m[p] <= n[p];
+    a.r = a.left ? n[p] : m[p];
+    a.c = a.left ? m[p] : n[p];
+    a.X = reinterpret_cast<T*>(base + L.X[p]);
+    a.V = reinterpret_cast<T*>(base + L.V[p]);
+    a.sig = reinterpret_cast<double*>(base + L.sig[p]);
+    a.sorted = reinterpret_cast<double*>(base + L.sorted[p]);
+    a.perm = reinterpret_cast<int*>(base + L.perm[p]);
+    a.info = reinterpret_cast<int*>(base + L.info[p]);
+    a.abs_floor = abs_floor;
+  }
+  DMRG_CUDA_TRY(cudaMemcpyAsync(base + L.tab, tab.data(), sizeof(BSvd<T>) * nprob, cudaMemcpyHostToDevice, s));
+  hestenes_batch_kernel<T><<<nprob, 1024, 0, s>>>(reinterpret_cast<const BSvd<T>*>(base + L.tab), 60);
+  DMRG_CHECK_LAUNCH();
+  std::vector<int> info(nprob);
+  for (int p = 0; p < nprob; ++p) {
+    const int c = tab[p].c;
+    DMRG_CUDA_TRY(cudaMemcpyAsync(host_s + (size_t)p * ld_s, tab[p].sorted, sizeof(double) * c,
+                                  cudaMemcpyDeviceToHost, s));
+    DMRG_CUDA_TRY(cudaMemcpyAsync(&info[p], tab[p].info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  int st = DMRG_OK;
+  for (int p = 0; p < nprob; ++p) {
+    for (int k = 0; k < tab[p].c; ++k) {
+      const double v = host_s[(size_t)p * ld_s + k];
+      if (!(v == v) || v > 1e300) return DMRG_ERR_NAN;
+    }
+    if (info[p] < 0) st = DMRG_ERR_NOCONV;
+  }
+  return st;
+}
+
+template <typename T>
+int hestenes_batch_output(int nprob, const int* m, const int* n, const int* keep, int absorb, void* work,
+                          T* const* lo, T* const* ro, cudaStream_t s) {
+  const BLayout L = batch_layout(sizeof(T), nprob, m, n, sizeof(BSvd<cplx>), sizeof(BOut<cplx>));
+  char* base = static_cast<char*>(work);
+  std::vector<BOut<T>> tab(nprob);
+  long long most = 1;
+  for (int p = 0; p < nprob; ++p) {
+    BOut<T>& o = tab[p];
+    o.X = reinterpret_cast<const T*>(base + L.X[p]);
+    o.V = reinterpret_cast<const T*>(base + L.V[p]);
+    o.perm = reinterpret_cast<const int*>(base + L.perm[p]);
+    o.sorted = reinterpret_cast<const double*>(base + L.sorted[p]);
+    o.m = m[p];
+    o.n = n[p];
+    o.left = m[p] <= n[p];
+    o.keep = keep[p];
+    o.lo = lo[p];
+    o.ro = ro[p];
+    const long long tot = (long long)m[p] * keep[p] + (long long)keep[p] * n[p];
+    if (tot > most) most = tot;
+  }
+  DMRG_CUDA_TRY(cudaMemcpyAsync(base + L.otab, tab.data(), sizeof(BOut<T>) * nprob, cudaMemcpyHostToDevice, s));
+  long long gx = (most + 255) / 256;
+  if (gx > 64) gx = 64;
+  if (nprob > 65535) return DMRG_ERR_ARG;
+  out_batch_kernel<T><<<dim3((unsigned)gx, (unsigned)nprob), 256, 0, s>>>(
+      reinterpret_cast<const BOut<T>*>(base + L.otab), absorb);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+template int hestenes_batch_factor<double>(int, const int*, const int*, const double* const*, void*, double*, int,
+                                           int, cudaStream_t);
+template int hestenes_batch_factor<cplx>(int, const int*, const int*, const cplx* const*, void*, double*, int, int,
+                                         cudaStream_t);
+template int hestenes_batch_output<double>(int, const int*, const int*, const int*, int, void*, double* const*,
+                                           double* const*, cudaStream_t);
+template int hestenes_batch_output<cplx>(int, const int*, const int*, const int*, int, void*, cplx* const*,
+                                         cplx* const*, cudaStream_t);
 
 template int hestenes_factor<double>(const double*, int, int, void*, double*, int*, int, cudaStream_t);
 template int hestenes_factor<cplx>(const cplx*, int, int, void*, double*, int*, int, cudaStream_t);

@@ -32,17 +32,15 @@ __device__ __forceinline__ long long off2(int i, int n2, long long s1, long long
   return (long long)q * s1 + (long long)r * s2;
 }
 
+// one BM x BN output tile (m0, n0) of batch entry bz
 template <typename T>
-__global__ void __launch_bounds__(NT) tgemm_kernel(Dev d, T alpha, const T* __restrict__ A,
-                                                   const T* __restrict__ B, T beta, T* __restrict__ C) {
+__device__ __forceinline__ void tgemm_tile(const Dev& d, T alpha, const T* __restrict__ A, const T* __restrict__ B,
+                                           T beta, T* __restrict__ C, int m0, int n0, int bz) {
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
   const int tid = threadIdx.x;
   const int tx = tid & 15;
   const int ty = tid >> 4;
-  const int m0 = blockIdx.x * BM;
-  const int n0 = blockIdx.y * BN;
-  const int bz = blockIdx.z;
   const int bq = bz / d.B2, br = bz - bq * d.B2;
   const T* Ab = A + (long long)bq * d.ab1 + (long long)br * d.ab2;
   const T* Bb = B + (long long)bq * d.bb1 + (long long)br * d.bb2;
@@ -114,11 +112,47 @@ __global__ void __launch_bounds__(NT) tgemm_kernel(Dev d, T alpha, const T* __re
   }
 }
 
-}  // namespace
+template <typename T>
+__global__ void __launch_bounds__(NT) tgemm_kernel(Dev d, T alpha, const T* __restrict__ A,
+                                                   const T* __restrict__ B, T beta, T* __restrict__ C) {
+  tgemm_tile<T>(d, alpha, A, B, beta, C, blockIdx.x * BM, blockIdx.y * BN, blockIdx.z);
+}
+
+// Grouped launch: problem p owns the flat tile range [start, start + tiles)
+// (tiles = batch * tiles_m * tiles_n); each CTA finds its problem by binary
+// search over the starts and runs one tile of it.
+struct GProb {
+  Dev d;
+  const void* A;
+  const void* B;
+  void* C;
+  int tiles_m, tiles_n;
+  long long start;
+};
 
 template <typename T>
-int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStream_t stream) {
-  Dev d;
+__global__ void __launch_bounds__(NT) tgemm_grouped_kernel(const GProb* __restrict__ probs, int nprob, T alpha,
+                                                           T beta) {
+  const long long t = blockIdx.x;
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].start <= t) lo = mid; else hi = mid - 1;
+  }
+  const GProb& g = probs[lo];
+  const long long local = t - g.start;
+  const long long per_b = (long long)g.tiles_m * g.tiles_n;
+  const int bz = (int)(local / per_b);
+  const int rem = (int)(local - (long long)bz * per_b);
+  const int tm = rem % g.tiles_m, tn = rem / g.tiles_m;
+  tgemm_tile<T>(g.d, alpha, static_cast<const T*>(g.A), static_cast<const T*>(g.B), beta, static_cast<T*>(g.C),
+                tm * BM, tn * BN, bz);
+}
+
+// Dev from a TGemm; returns false when there is nothing to do, *err on bad input
+bool make_dev(const TGemm& g, Dev* out, int* err) {
+  Dev& d = *out;
+  *err = DMRG_OK;
   const long long nb = (long long)g.B.n1 * g.B.n2;
   d.B2 = g.B.n2 > 0 ? g.B.n2 : 1;
   d.M = g.M.n1 * g.M.n2;
@@ -127,8 +161,11 @@ int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStr
   d.N2 = g.N.n2;
   d.K = g.K.n1 * g.K.n2;
   d.K2 = g.K.n2;
-  if (d.M <= 0 || d.N <= 0 || nb <= 0) return DMRG_OK;
-  if (d.M2 <= 0 || d.N2 <= 0 || d.K2 <= 0 || nb > 65535) return DMRG_ERR_ARG;
+  if (d.M <= 0 || d.N <= 0 || nb <= 0) return false;
+  if (d.M2 <= 0 || d.N2 <= 0 || d.K2 <= 0 || nb > 65535) {
+    *err = DMRG_ERR_ARG;
+    return false;
+  }
   d.ab1 = g.a_b.s1; d.ab2 = g.a_b.s2; d.am1 = g.a_m.s1; d.am2 = g.a_m.s2; d.ak1 = g.a_k.s1; d.ak2 = g.a_k.s2;
   d.bb1 = g.b_b.s1; d.bb2 = g.b_b.s2; d.bk1 = g.b_k.s1; d.bk2 = g.b_k.s2; d.bn1 = g.b_n.s1; d.bn2 = g.b_n.s2;
   d.cb1 = g.c_b.s1; d.cb2 = g.c_b.s2; d.cm1 = g.c_m.s1; d.cm2 = g.c_m.s2; d.cn1 = g.c_n.s1; d.cn2 = g.c_n.s2;
@@ -141,6 +178,17 @@ int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStr
   const long long bn_in = g.N.n2 == 1 ? g.b_n.s1 : g.b_n.s2;
   d.a_kfast = (ak_in == 1 && am_in != 1) ? 1 : 0;
   d.b_kfast = (bk_in == 1 && bn_in != 1) ? 1 : 0;
+  return true;
+}
+
+}  // namespace
+
+template <typename T>
+int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStream_t stream) {
+  Dev d;
+  int err = DMRG_OK;
+  if (!make_dev(g, &d, &err)) return err;
+  const long long nb = (long long)g.B.n1 * g.B.n2;
   dim3 grid((d.M + BM - 1) / BM, (d.N + BN - 1) / BN, (unsigned)nb);
   if (grid.y > 65535) return DMRG_ERR_ARG;
   tgemm_kernel<T><<<grid, NT, 0, stream>>>(d, alpha, A, B, beta, C);
@@ -148,7 +196,62 @@ int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStr
   return DMRG_OK;
 }
 
+size_t tgemm_grouped_desc_bytes(int nprob) { return align_up(sizeof(GProb) * (size_t)(nprob > 0 ? nprob : 1)); }
+
+int tgemm_grouped_build(int nprob, const TGemm* g, const void* const* A, const void* const* B, void* const* C,
+                        void* desc_host, int* nout, long long* tiles_out) {
+  GProb* h = static_cast<GProb*>(desc_host);
+  int n = 0;
+  long long tiles = 0;
+  for (int p = 0; p < nprob; ++p) {
+    Dev d;
+    int err = DMRG_OK;
+    if (!make_dev(g[p], &d, &err)) {
+      if (err != DMRG_OK) return err;
+      continue;
+    }
+    GProb& q = h[n++];
+    q.d = d;
+    q.A = A[p];
+    q.B = B[p];
+    q.C = C[p];
+    q.tiles_m = (d.M + BM - 1) / BM;
+    q.tiles_n = (d.N + BN - 1) / BN;
+    q.start = tiles;
+    tiles += (long long)g[p].B.n1 * g[p].B.n2 * q.tiles_m * q.tiles_n;
+  }
+  if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
+  *nout = n;
+  *tiles_out = tiles;
+  return DMRG_OK;
+}
+
+template <typename T>
+int tgemm_grouped_launch(const void* desc_dev, int n, long long tiles, T alpha, T beta, cudaStream_t stream) {
+  if (n == 0 || tiles == 0) return DMRG_OK;
+  tgemm_grouped_kernel<T><<<(unsigned)tiles, NT, 0, stream>>>(static_cast<const GProb*>(desc_dev), n, alpha, beta);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+template <typename T>
+int tgemm_grouped(int nprob, const TGemm* g, const void* const* A, const void* const* B, void* const* C, T alpha,
+                  T beta, void* desc_dev, void* desc_host, cudaStream_t stream) {
+  int n = 0;
+  long long tiles = 0;
+  DMRG_TRY(tgemm_grouped_build(nprob, g, A, B, C, desc_host, &n, &tiles));
+  if (n == 0) return DMRG_OK;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(desc_dev, desc_host, sizeof(GProb) * (size_t)n, cudaMemcpyHostToDevice, stream));
+  return tgemm_grouped_launch<T>(desc_dev, n, tiles, alpha, beta, stream);
+}
+
 template int tgemm<double>(const TGemm&, double, const double*, const double*, double, double*, cudaStream_t);
 template int tgemm<cplx>(const TGemm&, cplx, const cplx*, const cplx*, cplx, cplx*, cudaStream_t);
+template int tgemm_grouped_launch<double>(const void*, int, long long, double, double, cudaStream_t);
+template int tgemm_grouped_launch<cplx>(const void*, int, long long, cplx, cplx, cudaStream_t);
+template int tgemm_grouped<double>(int, const TGemm*, const void* const*, const void* const*, void* const*, double,
+                                   double, void*, void*, cudaStream_t);
+template int tgemm_grouped<cplx>(int, const TGemm*, const void* const*, const void* const*, void* const*, cplx, cplx,
+                                 void*, void*, cudaStream_t);
 
 }  // namespace dmrg

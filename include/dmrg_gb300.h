@@ -205,6 +205,45 @@ int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* s
                            int iters, void* left_out, void* right_out, double* discarded,
                            void* work, size_t work_bytes, void* stream);
 
+/* ---- many independent chains at once (FP64 / complex FP64) ----------------
+ * Batched forms of the bond-update steps for lock-step sweeps of nprob
+ * chains with different bond dimensions (one grouped launch per step).
+ * Per-problem shapes come as host arrays of length nprob and device
+ * pointers as host arrays of device addresses.  No reference counterpart:
+ * the reference sweeps one chain at a time; each batched step computes, per
+ * problem, what its single-chain entry point above computes. */
+size_t dmrg_batch_gemm_workspace_bytes(int nprob);
+/* C_p (m_p x n_p) = A_p (m_p x k_p) . B_p (k_p x n_p): the two-site merges. */
+int dmrg_batch_gemm(int dtype, int nprob, const int* m, const int* k, const int* n,
+                    const void* const* A, const void* const* B, void* const* C,
+                    void* work, size_t work_bytes, void* stream);
+/* side 0: Enew_p = dmrg_env_extend_left(E_p, W_p, A_p); side 1: right. */
+size_t dmrg_batch_env_workspace_bytes(int side, int dtype, int nprob, const int* chil, const int* d,
+                                      const int* chir, const int* wl, const int* wr);
+int dmrg_batch_env_extend(int side, int dtype, int nprob, const int* chil, const int* d, const int* chir,
+                          const int* wl, const int* wr, const void* const* E, const void* const* W,
+                          const void* const* A, void* const* Enew, void* work, size_t work_bytes, void* stream);
+/* dmrg_lanczos_ground for every ops[p] (kind 2, FP64 precision, one dtype),
+ * x[p] in/out; the recurrence runs in lock step, blocks of steps replayed
+ * from captured CUDA graphs when use_graph != 0 (cached per shape and
+ * workspace address); each problem stops by the single-chain rule, at most
+ * niter steps. */
+size_t dmrg_batch_lanczos_workspace_bytes(int nprob, const dmrg_heff_t* ops, int niter);
+int dmrg_batch_lanczos_ground(int nprob, const dmrg_heff_t* ops, void* const* x, int niter, double tol,
+                              int use_graph, double* energies, int* iters,
+                              void* work, size_t work_bytes, void* stream);
+/* dmrg_svd_truncate for every M_p (m_p x n_p) in two phases: factor (one CTA
+ * per problem) returns keep[p] by the truncation rule of
+ * pyitensor/svd.py:32-68 with maxdim[p]; the caller then allocates the
+ * outputs (m_p x keep_p, keep_p x n_p) and calls output with the same
+ * workspace and the same absorb. */
+size_t dmrg_batch_svd_workspace_bytes(int dtype, int nprob, const int* m, const int* n);
+int dmrg_batch_svd_factor(int dtype, int nprob, const int* m, const int* n, const void* const* M, double cutoff,
+                          const int* maxdim, int mindim, int absorb, int* keep, double* discarded, double* svals,
+                          int ld_svals, void* work, size_t work_bytes, void* stream);
+int dmrg_batch_svd_output(int dtype, int nprob, const int* m, const int* n, const int* keep, int absorb,
+                          void* const* left, void* const* right, void* work, size_t work_bytes, void* stream);
+
 /* ---- dense contraction ---------------------------------------------------- */
 size_t dmrg_gemm_workspace_bytes(int dtype, int precision, int m, int k, int n);
 /* C (m x n) = A (m x k) . B (k x n), all row-major.  Used for the two-site
