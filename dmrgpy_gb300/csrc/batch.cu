@@ -584,23 +584,15 @@ int dmrg_batch_svd_factor(int dtype, int nprob, const int* m, const int* n, cons
   }
   if (svals && ld_svals < cmax) return DMRG_ERR_ARG;
   if (svd_batch_work_bytes(dtype, nprob, m, n) > work_bytes) return DMRG_ERR_WORKSPACE;
-  // the divided factor need not be orthonormal (absorb 0 with X = M^H, absorb
-  // 1 with X = M) exactly when the single-problem driver enables the floor;
-  // a batch mixing both cases uses the safe setting
-  int floor_ok = 1;
-  for (int p = 0; p < nprob; ++p) {
-    const int left = m[p] <= n[p];
-    floor_ok = floor_ok && ((left && absorb == 0) || (!left && absorb == 1));
-  }
   std::vector<double> sv((size_t)nprob * cmax, 0.0);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int st;
   if (dtype == DMRG_COMPLEX128)
     st = hestenes_batch_factor<cplx>(nprob, m, n, reinterpret_cast<const cplx* const*>(M), work, sv.data(), cmax,
-                                     floor_ok, s);
+                                     absorb, s);
   else if (dtype == DMRG_REAL64)
     st = hestenes_batch_factor<double>(nprob, m, n, reinterpret_cast<const double* const*>(M), work, sv.data(), cmax,
-                                       floor_ok, s);
+                                       absorb, s);
   else
     return DMRG_ERR_ARG;
   if (st != DMRG_OK && st != DMRG_ERR_NOCONV) return st;

@@ -412,18 +412,14 @@ int svd_impl(int m, int n, const T* M, double cutoff, int maxdim, int mindim, in
   const int c = std::min(m, n);
   std::vector<double> sv(c);
   int sweeps = 0;
-  // the accumulated (exactly orthonormal) factor is U for m <= n, V otherwise;
-  // the absolute stop is safe when the caller does not need the other one
-  // to be orthonormal: absorb 0 keeps U orthonormal, absorb 1 keeps V
-  const bool left = m <= n;
-  const int abs_floor = (left && absorb == 0) || (!left && absorb == 1);
-  int st = hestenes_factor<T>(M, m, n, work, sv.data(), &sweeps, abs_floor, s);
+  const int left = svd_orientation_left(m, n, absorb);
+  int st = hestenes_factor<T>(M, m, n, left, work, sv.data(), &sweeps, svd_abs_floor(left, absorb), s);
   if (st != DMRG_OK && st != DMRG_ERR_NOCONV) return st;
   int kp;
   double dc;
   keep_rule(sv.data(), c, cutoff, maxdim, std::max(1, mindim), &kp, &dc);
   if (kp > c) kp = c;
-  DMRG_TRY(hestenes_output<T>(m, n, kp, absorb, work, lo, ro, s));
+  DMRG_TRY(hestenes_output<T>(m, n, left, kp, absorb, work, lo, ro, s));
   if (svals) std::memcpy(svals, sv.data(), sizeof(double) * c);
   if (keep) *keep = kp;
   if (disc) *disc = dc;

@@ -33,14 +33,19 @@ int env_right_fp64(long long cl, long long d, long long cr, long long wl, long l
 
 // truncated SVD (one-sided Jacobi)
 size_t svd_work_bytes(int dtype, int m, int n);
-template <typename T> int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, int abs_floor, cudaStream_t s);
-template <typename T> int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s);
+int svd_orientation_left(int m, int n, int absorb);
+int svd_abs_floor(int left, int absorb);
+template <typename T>
+int hestenes_factor(const T* M, int m, int n, int left, void* work, double* host_s, int* sweeps, int abs_floor,
+                    cudaStream_t s);
+template <typename T>
+int hestenes_output(int m, int n, int left, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s);
 
 // batched truncated SVD (one CTA per problem)
 size_t svd_batch_work_bytes(int dtype, int nprob, const int* m, const int* n);
 template <typename T>
 int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const* M, void* work, double* host_s,
-                          int ld_s, int abs_floor, cudaStream_t s);
+                          int ld_s, int absorb, cudaStream_t s);
 template <typename T>
 int hestenes_batch_output(int nprob, const int* m, const int* n, const int* keep, int absorb, void* work,
                           T* const* lo, T* const* ro, cudaStream_t s);

@@ -491,8 +491,8 @@ static SvdWork carve(void* work, int dtype, int m, int n) {
 // and copies them to host_s.  Returns DMRG_ERR_NOCONV if the sweep limit was
 // reached (the factorisation is still usable).
 template <typename T>
-int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* sweeps, int abs_floor, cudaStream_t s) {
-  const int left = m <= n;
+int hestenes_factor(const T* M, int m, int n, int left, void* work, double* host_s, int* sweeps, int abs_floor,
+                    cudaStream_t s) {
   const int r = left ? n : m;
   const int c = left ? m : n;
   SvdWork w = carve(work, sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64, m, n);
@@ -571,8 +571,7 @@ int hestenes_factor(const T* M, int m, int n, void* work, double* host_s, int* s
 }
 
 template <typename T>
-int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s) {
-  const int left = m <= n;
+int hestenes_output(int m, int n, int left, int keep, int absorb, void* work, T* lo, T* ro, cudaStream_t s) {
   SvdWork w = carve(work, sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64, m, n);
   long long tot = (long long)m * keep + (long long)keep * n;
   out_kernel<T><<<egrid(tot), 256, 0, s>>>(static_cast<const T*>(w.X), static_cast<const T*>(w.V), w.perm, w.sorted,
@@ -580,6 +579,16 @@ int hestenes_output(int m, int n, int keep, int absorb, void* work, T* lo, T* ro
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }
+
+// Which side Jacobi rotates: left (X = M^H, the accumulated rotations are U)
+// when m < n, right (X = M, rotations are V) when m > n; a square matrix
+// takes the side whose accumulated, exactly orthonormal, factor is the one
+// the caller keeps orthonormal (absorb 0: U, absorb 1: V).
+int svd_orientation_left(int m, int n, int absorb) { return m != n ? (m < n) : (absorb != 1); }
+// The absolute stop floor (couplings below 1e-16 |M|_F^2 are not rotated)
+// leaves the divided factor X/sigma orthonormal only to ~1e-16 |M|^2 /
+// (sigma_p sigma_q); it is safe when that factor is not the kept-orthonormal one.
+int svd_abs_floor(int left, int absorb) { return (left && absorb == 0) || (!left && absorb == 1); }
 
 // ---- batched host drivers
 namespace {
@@ -620,7 +629,7 @@ size_t svd_batch_work_bytes(int dtype, int nprob, const int* m, const int* n) {
 // host_s + p * ld_s.
 template <typename T>
 int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const* M, void* work, double* host_s,
-                          int ld_s, int abs_floor, cudaStream_t s) {
+                          int ld_s, int absorb, cudaStream_t s) {
   const BLayout L = batch_layout(sizeof(T), nprob, m, n, sizeof(BSvd<cplx>), sizeof(BOut<cplx>));
   char* base = static_cast<char*>(work);
   std::vector<BSvd<T>> tab(nprob);
@@ -629,7 +638,7 @@ int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const*
     a.M = M[p];
     a.m = m[p];
     a.n = n[p];
-    a.left = m[p] <= n[p];
+    a.left = svd_orientation_left(m[p], n[p], absorb);
     a.r = a.left ? n[p] : m[p];
     a.c = a.left ? m[p] : n[p];
     a.X = reinterpret_cast<T*>(base + L.X[p]);
@@ -638,7 +647,7 @@ int hestenes_batch_factor(int nprob, const int* m, const int* n, const T* const*
     a.sorted = reinterpret_cast<double*>(base + L.sorted[p]);
     a.perm = reinterpret_cast<int*>(base + L.perm[p]);
     a.info = reinterpret_cast<int*>(base + L.info[p]);
-    a.abs_floor = abs_floor;
+    a.abs_floor = svd_abs_floor(a.left, absorb);
   }
   DMRG_CUDA_TRY(cudaMemcpyAsync(base + L.tab, tab.data(), sizeof(BSvd<T>) * nprob, cudaMemcpyHostToDevice, s));
   hestenes_batch_kernel<T><<<nprob, 1024, 0, s>>>(reinterpret_cast<const BSvd<T>*>(base + L.tab), 60);
@@ -677,7 +686,7 @@ int hestenes_batch_output(int nprob, const int* m, const int* n, const int* keep
     o.sorted = reinterpret_cast<const double*>(base + L.sorted[p]);
     o.m = m[p];
     o.n = n[p];
-    o.left = m[p] <= n[p];
+    o.left = svd_orientation_left(m[p], n[p], absorb);
     o.keep = keep[p];
     o.lo = lo[p];
     o.ro = ro[p];
@@ -703,9 +712,9 @@ template int hestenes_batch_output<double>(int, const int*, const int*, const in
 template int hestenes_batch_output<cplx>(int, const int*, const int*, const int*, int, void*, cplx* const*,
                                          cplx* const*, cudaStream_t);
 
-template int hestenes_factor<double>(const double*, int, int, void*, double*, int*, int, cudaStream_t);
-template int hestenes_factor<cplx>(const cplx*, int, int, void*, double*, int*, int, cudaStream_t);
-template int hestenes_output<double>(int, int, int, int, void*, double*, double*, cudaStream_t);
-template int hestenes_output<cplx>(int, int, int, int, void*, cplx*, cplx*, cudaStream_t);
+template int hestenes_factor<double>(const double*, int, int, int, void*, double*, int*, int, cudaStream_t);
+template int hestenes_factor<cplx>(const cplx*, int, int, int, void*, double*, int*, int, cudaStream_t);
+template int hestenes_output<double>(int, int, int, int, int, void*, double*, double*, cudaStream_t);
+template int hestenes_output<cplx>(int, int, int, int, int, void*, cplx*, cplx*, cudaStream_t);
 
 }  // namespace dmrg

@@ -403,6 +403,77 @@ __global__ void __launch_bounds__(256) mpo_step_kernel(const float* __restrict__
   }
 }
 
+// Register-tiled form of the same step: warp al of the CTA owns a' = a0+al,
+// lane owns b = b0+lane; the thread keeps its (s,t,k) input column in
+// registers and reads each MPO row as broadcast float4s from shared memory,
+// so the loop is FMA-bound instead of shared-load-bound (one shared load per
+// four FMAs instead of two per FMA).  MAXC >= (d1 d2 wl) rounded up to 4.
+constexpr int RT_A = 8;
+
+template <int MAXC>
+__global__ void __launch_bounds__(256) mpo_step_rt_kernel(const float* __restrict__ X1, const float* __restrict__ W2,
+                                                          int chil, int d1, int d2, int chir, int wl, int wr, int Kp,
+                                                          float* __restrict__ hi, float* __restrict__ lo) {
+  extern __shared__ float4 sm4[];
+  float* sm = reinterpret_cast<float*>(sm4);
+  const int nst = d1 * d2;
+  const int in_cols = nst * wl;
+  const int out_rows = nst * wr;
+  const int cpad = (in_cols + 3) & ~3;
+  float* sW = sm;                        // out_rows x cpad, zero padded
+  float* sX = sW + out_rows * cpad;      // [al][c][32]
+  const int b0 = blockIdx.x * 32;
+  const int a0 = blockIdx.y * RT_A;
+  const long long ldx = (long long)chil * wl;
+  for (int i = threadIdx.x; i < out_rows * cpad; i += blockDim.x) {
+    const int r = i / cpad, c = i - r * cpad;
+    sW[i] = c < in_cols ? W2[r * in_cols + c] : 0.f;
+  }
+  const int ncolx = RT_A * wl;
+  for (int i = threadIdx.x; i < nst * 32 * ncolx; i += blockDim.x) {
+    const int col = i % ncolx;
+    const int bl = (i / ncolx) % 32;
+    const int st = i / (ncolx * 32);
+    const int al = col / wl, k = col - al * wl;
+    const int b = b0 + bl, a = a0 + al;
+    float v = 0.f;
+    if (b < chir && a < chil) v = X1[((long long)st * chir + b) * ldx + (long long)a * wl + k];
+    sX[(al * cpad + st * wl + k) * 32 + bl] = v;
+  }
+  for (int i = threadIdx.x; i < RT_A * (cpad - in_cols) * 32; i += blockDim.x) {
+    const int per = (cpad - in_cols) * 32;
+    const int al = i / per, rem = i - al * per;
+    sX[(al * cpad + in_cols + rem / 32) * 32 + (rem & 31)] = 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int al = threadIdx.x >> 5;
+  const int a = a0 + al, b = b0 + lane;
+  if (a >= chil || b >= chir) return;
+  float x[MAXC];
+#pragma unroll
+  for (int c = 0; c < MAXC; ++c) x[c] = c < cpad ? sX[(al * cpad + c) * 32 + lane] : 0.f;
+  for (int r = 0; r < out_rows; ++r) {
+    const float4* w4 = reinterpret_cast<const float4*>(sW + r * cpad);
+    float acc = 0.f;
+#pragma unroll
+    for (int c4 = 0; c4 < MAXC / 4; ++c4) {
+      if (c4 * 4 < cpad) {
+        const float4 w = w4[c4];
+        acc = fmaf(w.x, x[4 * c4 + 0], acc);
+        acc = fmaf(w.y, x[4 * c4 + 1], acc);
+        acc = fmaf(w.z, x[4 * c4 + 2], acc);
+        acc = fmaf(w.w, x[4 * c4 + 3], acc);
+      }
+    }
+    const int sp_tp = r / wr, n = r - sp_tp * wr;
+    const long long o = ((long long)a * nst + sp_tp) * Kp + (long long)n * chir + b;
+    const float h = to_tf32(acc);
+    hi[o] = h;
+    lo[o] = to_tf32(acc - h);
+  }
+}
+
 inline int egrid(long long n) {
   long long g = (n + 255) / 256;
   if (g > 152 * 16) g = 152 * 16;
@@ -516,6 +587,26 @@ Heff2Plan plan2(const dmrg_heff_t& o, void* work) {
   return p;
 }
 
+template <int MAXC>
+int launch_mpo_step_rt(const Heff2Plan& p, cudaStream_t s) {
+  const int nst = p.d1 * p.d2;
+  const int cpad = (nst * p.wl + 3) & ~3;
+  const size_t smem = sizeof(float) * ((size_t)nst * p.wr * cpad + (size_t)RT_A * cpad * 32);
+  if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
+  static bool attr = false;
+  if (!attr) {
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_rt_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       200 * 1024));
+    attr = true;
+  }
+  dim3 grid((p.cr + 31) / 32, (p.cl + RT_A - 1) / RT_A);
+  if (grid.y > 65535) return DMRG_ERR_ARG;
+  mpo_step_rt_kernel<MAXC><<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi,
+                                                   p.X3_lo);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
 }  // namespace
 
 size_t tf32x3_heff_workspace_bytes(const dmrg_heff_t& o) {
@@ -542,12 +633,30 @@ int tf32x3_heff_prepare(const dmrg_heff_t& o, void* work, cudaStream_t s) {
   return DMRG_OK;
 }
 
+int mpo_step_generic(const Heff2Plan& p, cudaStream_t s);
+
 int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s) {
   Heff2Plan p = plan2(o, work);
   // theta (cl, d1 d2 cr) -> thetaT rows (s,t,b), K = a
   DMRG_TRY(split_transpose(x, p.M1, p.cl, (int)p.M1, p.Kp1, p.thT_hi, p.thT_lo, s));
   GemmOut g1{p.X1, p.N1, 1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
   DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
+  const int nst = p.d1 * p.d2;
+  const int in_cols = nst * p.wl;
+  if (in_cols <= 48) {
+    DMRG_TRY(launch_mpo_step_rt<48>(p, s));
+  } else if (in_cols <= 96) {
+    DMRG_TRY(launch_mpo_step_rt<96>(p, s));
+  } else {
+    DMRG_TRY(mpo_step_generic(p, s));
+  }
+  GemmOut g4{y, p.cr, 1, (int)p.M4, p.cr, 1, 0, 1.f};
+  DMRG_TRY(gemm_split(p.X3_hi, p.X3_lo, p.R_hi, p.R_lo, (int)p.M4, p.cr, p.Kp4, g4, p.err, s));
+  return DMRG_OK;
+}
+
+// the shared-memory form for wide MPO steps (d1 d2 wl > 96)
+int mpo_step_generic(const Heff2Plan& p, cudaStream_t s) {
   const int nst = p.d1 * p.d2;
   const size_t smem = sizeof(float) * ((size_t)nst * p.wr * nst * p.wl + (size_t)MID_AT * nst * p.wl * 32);
   if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
@@ -560,8 +669,6 @@ int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y,
   if (grid.y > 65535) return DMRG_ERR_ARG;
   mpo_step_kernel<<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi, p.X3_lo);
   DMRG_CHECK_LAUNCH();
-  GemmOut g4{y, p.cr, 1, (int)p.M4, p.cr, 1, 0, 1.f};
-  DMRG_TRY(gemm_split(p.X3_hi, p.X3_lo, p.R_hi, p.R_lo, (int)p.M4, p.cr, p.Kp4, g4, p.err, s));
   return DMRG_OK;
 }
 
