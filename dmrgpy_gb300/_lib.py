@@ -80,6 +80,8 @@ SIGNATURES = [
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),
+    ("dmrg_autotune_enable", c_int, [c_int]),
+    ("dmrg_autotune_entries", c_int, [P_int, c_int]),
     ("dmrg_batch_gemm_workspace_bytes", c_size_t, [c_int]),
     ("dmrg_batch_gemm", c_int, [c_int, c_int, P_int, P_int, P_int, P_void, P_void, P_void, c_void_p, c_size_t,
                                 c_void_p]),

@@ -26,6 +26,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
+#include <map>
+#include <mutex>
+
 #include "tf32x3.cuh"
 
 namespace dmrg {
@@ -153,7 +157,7 @@ struct GemmOut {
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                        const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
-                       GemmOut out, int* err) {
+                       int tiles_m, int tiles_n, int group, GemmOut out, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
@@ -164,8 +168,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM;
-  const int n0 = blockIdx.y * BN;
+  // grouped tile order on a 1-D grid: consecutive CTAs walk `group` M-tiles
+  // for each N-tile, so the CTAs resident at one time share their operand
+  // panels in L2 (group = tiles_m is plain M-fastest order)
+  const int per_group = group * tiles_n;
+  const int gid = (int)blockIdx.x / per_group;
+  const int first_m = gid * group;
+  const int gsz = min(tiles_m - first_m, group);
+  const int local = (int)blockIdx.x - gid * per_group;
+  const int m0 = (first_m + local % gsz) * BM;
+  const int n0 = (local / gsz) * BN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -513,6 +525,45 @@ int make_map(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) 
 bool g_attr_set = false;
 
 // C (M x N) = A (M x Kp) . B (N x Kp)^T from split operands.
+// ---------------------------------------------------------------- tile-order tuner
+// Decisions per (device, M, N, Kp) of the split GEMM: the shapes of one
+// sweep are functions of (chi_l, chi_r, d, w), so a sweep tunes each of its
+// few shapes once.
+struct TuneKey {
+  int dev, M, N, K;
+  bool operator<(const TuneKey& o) const {
+    if (dev != o.dev) return dev < o.dev;
+    if (M != o.M) return M < o.M;
+    if (N != o.N) return N < o.N;
+    return K < o.K;
+  }
+};
+struct TuneVal {
+  int group;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+std::atomic<int> g_tune_on{1};
+
+TuneKey tune_key(int M, int N, int K) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return TuneKey{dev, M, N, K};
+}
+bool tune_enabled() { return g_tune_on.load() != 0; }
+bool tune_lookup(const TuneKey& k, int* group) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find(k);
+  if (it == g_tune.end()) return false;
+  *group = it->second.group;
+  return true;
+}
+void tune_store(const TuneKey& k, int group, float ms) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[k] = TuneVal{group, ms};
+}
+
 int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
                const GemmOut& out, int* err, cudaStream_t s) {
   DMRG_TRY(get_encoder());
@@ -525,11 +576,54 @@ int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float
     DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     g_attr_set = true;
   }
-  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
-  if (grid.y > 65535) return DMRG_ERR_ARG;
-  tf32x3_gemm_kernel<<<grid, GEMM_THREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, Kp / BK, out, err);
-  DMRG_CHECK_LAUNCH();
-  return DMRG_OK;
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+  const long long tiles = (long long)tiles_m * tiles_n;
+  if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
+  auto launch = [&](int group) -> int {
+    tf32x3_gemm_kernel<<<(unsigned)tiles, GEMM_THREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n,
+                                                                         group, out, err);
+    DMRG_CHECK_LAUNCH();
+    return DMRG_OK;
+  };
+  int group = tiles_m;
+  // Tile order is tuned per GEMM shape on its first overwrite-mode call
+  // (re-running an overwrite GEMM reproduces its output bit for bit: every
+  // tile sums the same K slices in the same order whatever the order of the
+  // tiles); accumulate-mode calls use the decision for their shape if one
+  // exists, else the plain order.
+  const TuneKey key = tune_key(M, N, Kp);
+  if (!tune_lookup(key, &group)) {
+    group = tiles_m;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    DMRG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+    if (tune_enabled() && !out.accumulate && cap == cudaStreamCaptureStatusNone && tiles >= 2 * 152) {
+      const int cand[4] = {tiles_m, 16, 8, 4};
+      float best = 0.f;
+      cudaEvent_t e0, e1;
+      DMRG_CUDA_TRY(cudaEventCreate(&e0));
+      DMRG_CUDA_TRY(cudaEventCreate(&e1));
+      for (int i = 0; i < 4; ++i) {
+        const int g = cand[i] < tiles_m ? cand[i] : tiles_m;
+        if (i > 0 && g == tiles_m) continue;
+        DMRG_TRY(launch(g));  // warm
+        DMRG_CUDA_TRY(cudaEventRecord(e0, s));
+        DMRG_TRY(launch(g));
+        DMRG_CUDA_TRY(cudaEventRecord(e1, s));
+        DMRG_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        DMRG_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (i == 0 || ms < best) {
+          best = ms;
+          group = g;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      tune_store(key, group, best);
+      return launch(group);
+    }
+  }
+  return launch(group);
 }
 
 int split_rows(const double* in, long long ldr, long long ldk, int R, int K, int Kp, float* hi, float* lo,
@@ -953,3 +1047,23 @@ int tf32x3_env(int side, int cl, int d, int cr, int wl, int wr, const double* E,
 }
 
 }  // namespace dmrg
+
+// ---------------------------------------------------------------- C ABI of the tuner
+extern "C" int dmrg_autotune_enable(int enable) { return dmrg::g_tune_on.exchange(enable ? 1 : 0); }
+
+extern "C" int dmrg_autotune_entries(int* out, int max_entries) {
+  std::lock_guard<std::mutex> lock(dmrg::g_tune_mu);
+  int n = 0;
+  for (const auto& kv : dmrg::g_tune) {
+    if (out && n < max_entries) {
+      int* e = out + 5 * n;
+      e[0] = kv.first.M;
+      e[1] = kv.first.N;
+      e[2] = kv.first.K;
+      e[3] = kv.second.group;
+      e[4] = (int)(kv.second.ms * 1000.f);
+    }
+    ++n;
+  }
+  return n;
+}

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from golden_data import terms_heisenberg
+from golden_data import meta, terms_heisenberg
 
 pytestmark = pytest.mark.gpu
 
@@ -19,18 +19,25 @@ def _engine(W, precision):
 
 def _mpo_pair(code):
     from dmrgpy_gb300 import mpo as M
+    if code == "hubbard":
+        # spinful fermions, d = 4: the two-site MPO step is 96 wide
+        md = meta()
+        W, real = M.build_mpo(md["types"]["hubbard4"], md["terms"]["hubbard4"])
+        assert real
+        return W[1], W[2]
     W, real = M.build_mpo([code] * 6, terms_heisenberg(6))
     assert real
     return W[2], W[3]
 
 
-@pytest.mark.parametrize("chil,chir,code", [(96, 96, 2), (64, 160, 3), (256, 256, 3), (37, 45, 2)])
+@pytest.mark.parametrize("chil,chir,code", [(96, 96, 2), (64, 160, 3), (256, 256, 3), (37, 45, 2),
+                                            (64, 72, "hubbard")])
 def test_tf32x3_two_site_matvec(chil, chir, code):
     rng = np.random.default_rng(chil * 7 + chir)
     Wi, Wj = _mpo_pair(code)
-    d, w = Wi.shape[1], Wi.shape[3]
-    L = rng.standard_normal((chil, w, chil))
-    R = rng.standard_normal((chir, w, chir))
+    d = Wi.shape[1]
+    L = rng.standard_normal((chil, Wi.shape[0], chil))
+    R = rng.standard_normal((chir, Wj.shape[3], chir))
     th = rng.standard_normal((chil, d, d, chir))
     ref = O.heff2_matvec(L, Wi, Wj, R, th).real
     eng = _engine([Wi, Wj], "tf32x3")
@@ -75,3 +82,32 @@ def test_tf32x3_lanczos_energy_close_to_fp64():
         e, k = eng.ground(h, thd, 200)
         out[prec] = e
     assert abs(out["tf32x3"] - out["fp64"]) <= 1e-5 * abs(out["fp64"])
+
+
+def test_gemm_tile_order_tuner_changes_nothing_but_speed():
+    """The tuner picks a tile order per GEMM shape; every order gives the
+    same bits, so tuned and untuned runs must agree exactly."""
+    import ctypes
+    from dmrgpy_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(11)
+    m, k, n = 2560, 512, 2560          # 400 output tiles: large enough to be tuned
+    A = rng.standard_normal((m, k))
+    B = rng.standard_normal((k, n))
+    eng = _engine([np.zeros((1, 2, 2, 1))], "tf32x3")
+    Ad, Bd = eng.to_device([A, B])
+    prev = lib.dmrg_autotune_enable(0)
+    try:
+        C0 = eng.gemm(Ad, Bd).cpu().numpy()
+        lib.dmrg_autotune_enable(1)
+        C1 = eng.gemm(Ad, Bd).cpu().numpy()      # first call of the shape: tuned
+        C2 = eng.gemm(Ad, Bd).cpu().numpy()      # uses the decision
+    finally:
+        lib.dmrg_autotune_enable(prev)
+    assert np.array_equal(C0, C1) and np.array_equal(C1, C2)
+    count = lib.dmrg_autotune_entries(None, 0)
+    buf = (ctypes.c_int * (5 * max(count, 1)))()
+    lib.dmrg_autotune_entries(buf, count)
+    shapes = [tuple(buf[5 * i:5 * i + 4]) for i in range(count)]
+    assert any(s[0] == m and s[1] == n for s in shapes), shapes
+    assert np.max(np.abs(C1 - A @ B)) / np.max(np.abs(A @ B)) < TOL
