@@ -292,6 +292,40 @@ def run_gpu(args):
             "tf32x3_ceiling_tflops": bf16 / 2.0 / 3.0,
             "frac_of_tf32x3_ceiling": achieved / (bf16 / 2.0 / 3.0)}
 
+    # --- the FP64 GPU path on the same chi=1024 bond (the metric's comparison):
+    # one FP64 bond update = mean-iterations FP64 matvecs + FP64 Jacobi
+    # truncation + FP64 environment extension, each timed with CUDA events;
+    # a full FP64 sweep is that bond time x the bond updates of a sweep
+    fp64 = None
+    if not args.no_fp64:
+        e64 = Engine(W, real=real, precision="fp64", device="cuda:%d" % local)
+        h64 = e64.heff2(lenv[mid - 1], e64.W[mid - 1], e64.W[mid], renv[mid + 2], theta.shape)
+
+        def timed(fn, reps=1):
+            fn()
+            torch.cuda.synchronize()
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record()
+            for _ in range(reps):
+                fn()
+            a1.record()
+            torch.cuda.synchronize()
+            return a0.elapsed_time(a1) / 1e3 / reps
+
+        t64_mv = timed(lambda: e64.apply(h64, theta), 2)
+        m2 = cl * d1
+        t64_svd = timed(lambda: e64.svd(theta.view(m2, -1), 0.0, CHI, 1, 0))
+        t64_env = timed(lambda: e64.env_left(lenv[mid - 1], e64.W[mid - 1], A[mid - 1], fp64=True))
+        k_mean = float(np.mean(iters)) if iters else 3.0
+        bond64 = k_mean * t64_mv + t64_svd + t64_env
+        nb = len(st.records) / max(1, args.steps)
+        fp64 = {"matvec_s": t64_mv, "svd_s": t64_svd, "env_s": t64_env, "bond_s": bond64,
+                "sweep_s_est": bond64 * nb, "speedup_vs_fp64_est": bond64 * nb / (elapsed / args.steps),
+                "note": "FP64 GPU bond update at the chi=1024 middle bond (same state), times the %d bond "
+                        "updates of a sweep; matvec count = mean Lanczos iterations of the split-TF32 sweep" % nb}
+        del e64, h64
+
     # --- FP64 refinement of the energy of the final state (not in the timed steps)
     t0 = time.perf_counter()
     e_ref = eng.energy_fp64(A)
@@ -323,7 +357,7 @@ def run_gpu(args):
                                    "(ramp 64->256->1024, cutoff 0), split-TF32 + FP64 refine",
                        "chi": CHI, "n_sites": N_SITES, "d": D, "w": 5, "l2": "working set >> L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "clocks": clk, "gpu_launches": int(launches), "e2e": e2e, "roofline": roof,
+            "clocks": clk, "gpu_launches": int(launches), "e2e": e2e, "roofline": roof, "fp64_gpu": fp64,
             "sweep": {"sweep_s": elapsed / args.steps, "wall_s": t_wall / args.steps,
                       "phase_s": {k: v / args.steps for k, v in st.t.items()},
                       "matvecs_per_sweep": st.matvecs / args.steps,
@@ -358,6 +392,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU bond sample")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
