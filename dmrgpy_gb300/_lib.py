@@ -65,6 +65,10 @@ SIGNATURES = [
     ("dmrg_env_gradient_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int, c_int]),
     ("dmrg_env_gradient", c_int, [c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                   c_void_p, c_size_t, c_void_p]),
+    ("dmrg_env_mixed_workspace_bytes", c_size_t, [c_int] * 9),
+    ("dmrg_env_extend_mixed", c_int, [c_int] * 9 + [c_void_p] * 6 + [c_size_t, c_void_p]),
+    ("dmrg_env_gradient_mixed_workspace_bytes", c_size_t, [c_int] * 8),
+    ("dmrg_env_gradient_mixed", c_int, [c_int] * 8 + [c_void_p] * 6 + [c_size_t, c_void_p]),
     ("dmrg_lanczos_workspace_bytes", c_size_t, [ctypes.POINTER(HeffDesc), c_int]),
     ("dmrg_lanczos_ground", c_int, [ctypes.POINTER(HeffDesc), c_void_p, c_int, c_double, P_double, P_int,
                                     c_void_p, c_size_t, c_void_p]),

@@ -288,6 +288,59 @@ class Engine:
             ptr, size, self.stream))
         return out
 
+    # ------------------------------------------------------------ transition forms
+    def env_mixed(self, side, E, W, B, A):
+        """Transition environment with bra B and ket A (side 0: left, 1: right), FP64."""
+        torch = _torch()
+        clb, d, crb = B.shape
+        clk, _, crk = A.shape
+        wl, wr = W.shape[0], W.shape[3]
+        shape = (crb, wr, crk) if side == 0 else (clb, wl, clk)
+        out = torch.empty(shape, dtype=self.tdtype, device=self.device)
+        need = self.lib.dmrg_env_mixed_workspace_bytes(side, self.cdtype, clb, crb, clk, crk, d, wl, wr)
+        ptr, size = self.ws.get(need)
+        _lib.check("dmrg_env_extend_mixed", self.lib.dmrg_env_extend_mixed(
+            side, self.cdtype, clb, crb, clk, crk, d, wl, wr, E.data_ptr(), W.data_ptr(), B.data_ptr(),
+            A.data_ptr(), out.data_ptr(), ptr, size, self.stream))
+        return out
+
+    def transition_gradients(self, Bra, Ket):
+        """<bra|H|ket> and G_i = d<bra|H|ket>/dW_i for every site (FP64, no
+        normalisation): the adjoint pass of mpo_gradients with two states."""
+        torch = _torch()
+        n = len(Ket)
+        R = {n + 1: self.edge}
+        for i in range(n, 1, -1):
+            R[i] = self.env_mixed(1, R[i + 1], self.W[i - 1], Bra[i - 1], Ket[i - 1])
+        L = self.edge
+        grads = []
+        for i in range(n):
+            W = self.W[i]
+            B, A = Bra[i], Ket[i]
+            clb, d, crb = B.shape
+            clk, _, crk = A.shape
+            wl, wr = W.shape[0], W.shape[3]
+            G = torch.empty((wl, d, d, wr), dtype=self.tdtype, device=self.device)
+            need = self.lib.dmrg_env_gradient_mixed_workspace_bytes(self.cdtype, clb, crb, clk, crk, d, wl, wr)
+            ptr, size = self.ws.get(need)
+            _lib.check("dmrg_env_gradient_mixed", self.lib.dmrg_env_gradient_mixed(
+                self.cdtype, clb, crb, clk, crk, d, wl, wr, L.data_ptr(), B.data_ptr(), A.data_ptr(),
+                R[i + 2].data_ptr(), G.data_ptr(), ptr, size, self.stream))
+            grads.append(G)
+            L = self.env_mixed(0, L, W, B, A)
+        return complex(L.reshape(-1)[0].item()), grads
+
+    def right_canonicalize(self, A):
+        """Lossless right-to-left SVD pass: A[1:] right-orthonormal, the
+        norm carried into A[0] (the gauge the TDVP sweep starts from)."""
+        for i in range(len(A) - 1, 0, -1):
+            cl, d, cr = A[i].shape
+            lo, ro, _, k, _ = self.svd(A[i].reshape(cl, d * cr), 0.0, 0, 1, 1)
+            A[i] = ro.reshape(k, d, cr)
+            prv = A[i - 1]
+            A[i - 1] = self.gemm(prv.reshape(-1, cl), lo).reshape(prv.shape[0], prv.shape[1], k)
+        return A
+
     def set_mpo(self, W):
         """Replace the MPO tensors (same shapes), e.g. after a change of couplings."""
         torch = _torch()

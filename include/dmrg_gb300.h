@@ -141,6 +141,25 @@ int dmrg_env_gradient(int dtype, int chil, int d, int chir, int wl, int wr,
                       const void* L, const void* A, const void* R, void* G,
                       void* work, size_t work_bytes, void* stream);
 
+/* Transition forms for <chi|H|psi> with two different MPS: bra B (clb, d,
+ * crb), ket A (clk, d, crk), environments (chi_bra, w, chi_ket).
+ * side 0: Lnew (crb, wr, crk) = L (clb, wl, clk) . conj(B) . W . A;
+ * side 1: Rnew (clb, wl, clk) = R (crb, wr, crk) . conj(B) . W . A.
+ * Used by the adjoint of real-time evolution (costate bra, state ket); the
+ * reference's counterpart is its transition element overlap_aMb
+ * (pyitensor/chain.py:289-293), evaluated there on the host. */
+size_t dmrg_env_mixed_workspace_bytes(int side, int dtype, int clb, int crb, int clk, int crk, int d, int wl, int wr);
+int dmrg_env_extend_mixed(int side, int dtype, int clb, int crb, int clk, int crk, int d, int wl, int wr,
+                          const void* E, const void* W, const void* B, const void* A, void* Enew,
+                          void* work, size_t work_bytes, void* stream);
+/* G (wl, d, d, wr) = d<chi|H|psi>/dW_i with the bra/ket site tensors B, A and
+ * the transition environments L (clb, wl, clk), R (crb, wr, crk).  No
+ * reference counterpart (no derivative features in the reference). */
+size_t dmrg_env_gradient_mixed_workspace_bytes(int dtype, int clb, int crb, int clk, int crk, int d, int wl, int wr);
+int dmrg_env_gradient_mixed(int dtype, int clb, int crb, int clk, int crk, int d, int wl, int wr,
+                            const void* L, const void* B, const void* A, const void* R, void* G,
+                            void* work, size_t work_bytes, void* stream);
+
 /* ---- Krylov solvers ------------------------------------------------------ */
 size_t dmrg_lanczos_workspace_bytes(const dmrg_heff_t* op, int niter);
 /* Lowest eigenpair of H_eff by Lanczos with full reorthogonalisation; stops
