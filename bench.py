@@ -190,7 +190,7 @@ def run_gpu(args):
     from dmrgpy_gb300 import _lib
     from dmrgpy_gb300 import mpo as M
     from dmrgpy_gb300 import mps as MP
-    from dmrgpy_gb300.engine import Engine
+    from dmrgpy_gb300.engine import Engine, SweepStats
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -216,7 +216,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    eng.stats.__init__()
+    eng.stats = SweepStats()
     clocks = ClockSampler()
     clocks.start()
     l0 = lib.dmrg_kernel_launches()
@@ -336,7 +336,7 @@ def run_gpu(args):
     h2d = sum(a.nbytes for a in host)
     pinned = [torch.from_numpy(a).pin_memory() for a in host]
     eng.invalidate()
-    eng.stats.__init__()
+    eng.stats = SweepStats()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     Ad = [p.to(eng.device, non_blocking=True) for p in pinned]
