@@ -135,6 +135,9 @@ int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStr
 // Many strided contractions of different shapes in one launch.  desc_host
 // (pageable, tgemm_grouped_desc_bytes(nprob)) stages the problem table that
 // is copied to desc_dev (device, same size) on the stream.
+// G (k x k) = X^T X for X (m x k, row stride ld), FP64: only the upper
+// triangle of output tiles is computed, each off-diagonal tile written twice.
+int tgemm_gram(const double* X, long long ld, int m, int k, double* G, cudaStream_t stream);
 size_t tgemm_grouped_desc_bytes(int nprob);
 // the same split in two: the problem table built on the host (desc_host),
 // then -- after the caller has copied it to device memory -- the launch

@@ -187,12 +187,7 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
 // because E is already tiny.
 int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* B, unsigned long long* dev, void* gw,
                       int* err, cudaStream_t s) {
-  TGemm g{};
-  g.B = ax(1); g.M = ax(k); g.K = ax(m); g.N = ax(k);
-  g.a_m = st(1); g.a_k = st(ld);
-  g.b_k = st(ld); g.b_n = st(1);
-  g.c_m = st(k); g.c_n = st(1);
-  DMRG_TRY(tgemm<double>(g, 1.0, Z, Z, 0.0, A, s));
+  DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
   poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
   DMRG_CHECK_LAUNCH();

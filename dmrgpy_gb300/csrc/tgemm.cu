@@ -33,7 +33,9 @@ __device__ __forceinline__ long long off2(int i, int n2, long long s1, long long
 }
 
 // one BM x BN output tile (m0, n0) of batch entry bz
-template <typename T>
+// MIRROR: C is square with equal M and N layouts and the product is
+// symmetric (C = X^T X); an off-diagonal tile also writes its transpose.
+template <typename T, bool MIRROR = false>
 __device__ __forceinline__ void tgemm_tile(const Dev& d, T alpha, const T* __restrict__ A, const T* __restrict__ B,
                                            T beta, T* __restrict__ C, int m0, int n0, int bz) {
   __shared__ T As[BK][BM + 1];
@@ -108,8 +110,23 @@ __device__ __forceinline__ void tgemm_tile(const Dev& d, T alpha, const T* __res
       T v = Sc<T>::mul(alpha, acc[i][j]);
       if (use_beta) v = Sc<T>::fma(beta, Cb[o], v);
       Cb[o] = v;
+      if (MIRROR && m0 != n0) Cb[off2(gn, d.M2, d.cm1, d.cm2) + off2(gm, d.N2, d.cn1, d.cn2)] = v;
     }
   }
+}
+
+// Symmetric product: only the tiles with tile row <= tile column, numbered
+// row by row over the upper triangle of a tiles x tiles grid.
+template <typename T>
+__global__ void __launch_bounds__(NT) tgemm_sym_kernel(Dev d, T alpha, const T* __restrict__ A,
+                                                       const T* __restrict__ B, T* __restrict__ C, int tiles) {
+  int rem = blockIdx.x, tm = 0;
+  while (tm < tiles && rem >= tiles - tm) {
+    rem -= tiles - tm;
+    ++tm;
+  }
+  if (tm >= tiles) return;
+  tgemm_tile<T, true>(d, alpha, A, B, Sc<T>::zero(), C, tm * BM, (tm + rem) * BN, 0);
 }
 
 template <typename T>
@@ -192,6 +209,24 @@ int tgemm(const TGemm& g, T alpha, const T* A, const T* B, T beta, T* C, cudaStr
   dim3 grid((d.M + BM - 1) / BM, (d.N + BN - 1) / BN, (unsigned)nb);
   if (grid.y > 65535) return DMRG_ERR_ARG;
   tgemm_kernel<T><<<grid, NT, 0, stream>>>(d, alpha, A, B, beta, C);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
+
+int tgemm_gram(const double* X, long long ld, int m, int k, double* G, cudaStream_t stream) {
+  if (m < 1 || k < 1) return DMRG_ERR_ARG;
+  TGemm g{};
+  g.B = ax(1); g.M = ax(k); g.K = ax(m); g.N = ax(k);
+  g.a_m = st(1); g.a_k = st(ld);
+  g.b_k = st(ld); g.b_n = st(1);
+  g.c_m = st(k); g.c_n = st(1);
+  Dev d;
+  int err = DMRG_OK;
+  if (!make_dev(g, &d, &err)) return err;
+  const int tiles = (k + BM - 1) / BM;
+  const long long ntri = (long long)tiles * (tiles + 1) / 2;
+  if (ntri > 0x7fffffffLL) return DMRG_ERR_ARG;
+  tgemm_sym_kernel<double><<<(unsigned)ntri, NT, 0, stream>>>(d, 1.0, X, X, G, tiles);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }

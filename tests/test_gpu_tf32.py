@@ -111,3 +111,34 @@ def test_gemm_tile_order_tuner_changes_nothing_but_speed():
     shapes = [tuple(buf[5 * i:5 * i + 4]) for i in range(count)]
     assert any(s[0] == m and s[1] == n for s in shapes), shapes
     assert np.max(np.abs(C1 - A @ B)) / np.max(np.abs(A @ B)) < TOL
+
+
+@pytest.mark.parametrize("absorb", [0, 1])
+def test_subspace_truncation_is_orthonormal_and_near_optimal(absorb):
+    """Fixed-rank truncation by subspace iteration from a warm start (the
+    orthonormal tensor across the bond, here the exact singular vectors
+    perturbed by 1e-3): the kept basis is orthonormal to FP64 level (FP64-Gram
+    correction) and the discarded weight is within 10% of the SVD optimum."""
+    rng = np.random.default_rng(21 + absorb)
+    m = n = 576
+    k = 256
+    U, _ = np.linalg.qr(rng.standard_normal((m, m)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.exp(-12.0 * np.arange(m) / m)
+    th = (U * s) @ V.T
+    opt = np.sqrt(np.sum(s[k:] ** 2) / np.sum(s ** 2))
+    if absorb == 0:
+        start, _ = np.linalg.qr(V[:, :k] + 1e-3 * rng.standard_normal((n, k)))
+        start = np.ascontiguousarray(start.T)          # k x n, orthonormal rows
+    else:
+        start, _ = np.linalg.qr(U[:, :k] + 1e-3 * rng.standard_normal((m, k)))
+        start = np.ascontiguousarray(start)            # m x k, orthonormal columns
+    eng = _engine([np.zeros((1, 2, 2, 1))], "tf32x3")
+    thd, std = eng.to_device([th, start])
+    lo, ro, _, kk, disc = eng.subspace_split(thd, k, std, k, absorb)
+    lo, ro = lo.cpu().numpy(), ro.cpu().numpy()
+    Q = lo if absorb == 0 else ro.T
+    assert np.max(np.abs(Q.T @ Q - np.eye(k))) < 1e-10
+    rec = np.linalg.norm(lo @ ro - th) / np.linalg.norm(th)
+    assert rec < 1.1 * opt, (rec, opt)
+    assert abs(disc - rec ** 2) < 1e-3 * rec ** 2 + 1e-12
