@@ -270,19 +270,52 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
     }
     const int gm = m0 + row;
-    if (ok && gm < out.M) {
+    // full-width tiles of row-contiguous outputs are written with 16-byte
+    // stores (4 floats / 2+2 doubles per step) instead of one element
+    const bool inrow = ok && gm < out.M;
+    const bool vec = inrow && out.ldn == 1 && n0 + BN <= out.N &&
+                     ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
+                     (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
+    if (inrow) {
+      const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
-      for (int c = 0; c < BN; ++c) {
-        const int gn = n0 + c;
-        if (gn < out.N) {
-          const long long o = (long long)gm * out.ldm + (long long)gn * out.ldn;
-          const float r = out.alpha * acc[c];
+      for (int c = 0; c < BN; c += 4) {
+        const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
+        const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
+        if (vec) {
           if (out.out_f64) {
-            double* C = static_cast<double*>(out.C);
-            C[o] = out.accumulate ? C[o] + (double)r : (double)r;
+            double2* p = reinterpret_cast<double2*>(static_cast<double*>(out.C) + rowoff + n0 + c);
+            double2 u = make_double2(r0, r1), v = make_double2(r2, r3);
+            if (out.accumulate) {
+              const double2 pu = p[0], pv = p[1];
+              u.x += pu.x; u.y += pu.y; v.x += pv.x; v.y += pv.y;
+            }
+            p[0] = u;
+            p[1] = v;
           } else {
-            float* C = static_cast<float*>(out.C);
-            C[o] = out.accumulate ? C[o] + r : r;
+            float4* p = reinterpret_cast<float4*>(static_cast<float*>(out.C) + rowoff + n0 + c);
+            float4 u = make_float4(r0, r1, r2, r3);
+            if (out.accumulate) {
+              const float4 o = *p;
+              u.x += o.x; u.y += o.y; u.z += o.z; u.w += o.w;
+            }
+            *p = u;
+          }
+        } else {
+          const float rr[4] = {r0, r1, r2, r3};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + c + j;
+            if (gn < out.N) {
+              const long long o = rowoff + (long long)gn * out.ldn;
+              if (out.out_f64) {
+                double* C = static_cast<double*>(out.C);
+                C[o] = out.accumulate ? C[o] + (double)rr[j] : (double)rr[j];
+              } else {
+                float* C = static_cast<float*>(out.C);
+                C[o] = out.accumulate ? C[o] + rr[j] : rr[j];
+              }
+            }
           }
         }
       }
