@@ -174,8 +174,18 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
     B[i] = b * a + (r == cc ? c : 0.0);
     mx = fmax(mx, fabs(a - (r == cc ? 1.0 : 0.0)));
   }
-  // max of non-negative doubles via their bit patterns
-  atomicMax(dev, __double_as_longlong(mx));
+  // block max first, then one atomic per block (max of non-negative doubles
+  // via their bit patterns): a per-thread atomic on one address serialises
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    atomicMax(dev, __double_as_longlong(m));
+  }
 }
 
 // The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
