@@ -247,8 +247,12 @@ class Engine:
         return lo, ro, None, k, disc.value
 
     def use_subspace(self, m, n, cutoff, maxdim):
-        return (self.prec == _lib.PREC_TF32X3 and self.real and cutoff <= 0.0 and maxdim and maxdim > 0
-                and min(m, n) >= SUBSPACE_MIN_DIM)
+        """Split-TF32 sweeps with a maxdim-bound truncation use the fixed-rank
+        path: subspace iteration for large bonds, and for any size when the
+        kept rank is the full min(m, n) (then the subspace is exact)."""
+        if not (self.prec == _lib.PREC_TF32X3 and self.real and cutoff <= 0.0 and maxdim and maxdim > 0):
+            return False
+        return min(m, n) >= SUBSPACE_MIN_DIM or min(maxdim, m, n) == min(m, n)
 
     def env_left(self, L, W, A, fp64=False):
         torch = _torch()
@@ -413,8 +417,15 @@ class Engine:
         t2 = time.perf_counter()
         cl, d1, d2, cr = theta.shape
         m, n = cl * d1, d2 * cr
-        if self.use_subspace(m, n, cutoff, maxdim):
-            rank = min(maxdim, m, n)
+        rank = min(maxdim, m, n) if maxdim and maxdim > 0 else min(m, n)
+        if self.use_subspace(m, n, cutoff, maxdim) and ((absorb == 0 and rank == m) or (absorb == 1 and rank == n)):
+            # nothing to truncate on the kept side: the identity is an exact
+            # orthonormal basis of it and theta itself the other factor
+            eye = torch.eye(rank, dtype=self.tdtype, device=self.device)
+            tm = theta.view(m, n)
+            lo, ro = (eye, tm) if absorb == 0 else (tm, eye)
+            s, keep, disc = None, rank, 0.0
+        elif self.use_subspace(m, n, cutoff, maxdim):
             # warm start: the orthonormal tensor on the other side of the bond
             # (right-canonical A_j in a left-to-right pass, left-canonical A_i
             # in a right-to-left pass)
