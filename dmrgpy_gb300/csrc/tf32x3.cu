@@ -466,7 +466,8 @@ __global__ void __launch_bounds__(256) mpo_step_rt_kernel(const float* __restric
   const int out_rows = nst * wr;
   const int cpad = (in_cols + 3) & ~3;
   float* sW = sm;                        // out_rows x cpad, zero padded
-  float* sX = sW + out_rows * cpad;      // [al][c][32]
+  float* sX = sW + out_rows * cpad;      // [al][c][33]: row stride 33 keeps the
+                                         // staging stores free of bank conflicts
   const int b0 = blockIdx.x * 32;
   const int a0 = blockIdx.y * RT_A;
   const long long ldx = (long long)chil * wl;
@@ -483,12 +484,12 @@ __global__ void __launch_bounds__(256) mpo_step_rt_kernel(const float* __restric
     const int b = b0 + bl, a = a0 + al;
     float v = 0.f;
     if (b < chir && a < chil) v = X1[((long long)st * chir + b) * ldx + (long long)a * wl + k];
-    sX[(al * cpad + st * wl + k) * 32 + bl] = v;
+    sX[(al * cpad + st * wl + k) * 33 + bl] = v;
   }
   for (int i = threadIdx.x; i < RT_A * (cpad - in_cols) * 32; i += blockDim.x) {
     const int per = (cpad - in_cols) * 32;
     const int al = i / per, rem = i - al * per;
-    sX[(al * cpad + in_cols + rem / 32) * 32 + (rem & 31)] = 0.f;
+    sX[(al * cpad + in_cols + rem / 32) * 33 + (rem & 31)] = 0.f;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(256) mpo_step_rt_kernel(const float* __restric
   if (a >= chil || b >= chir) return;
   float x[MAXC];
 #pragma unroll
-  for (int c = 0; c < MAXC; ++c) x[c] = c < cpad ? sX[(al * cpad + c) * 32 + lane] : 0.f;
+  for (int c = 0; c < MAXC; ++c) x[c] = c < cpad ? sX[(al * cpad + c) * 33 + lane] : 0.f;
   for (int r = 0; r < out_rows; ++r) {
     const float4* w4 = reinterpret_cast<const float4*>(sW + r * cpad);
     float acc = 0.f;
@@ -718,7 +719,7 @@ template <int MAXC>
 int launch_mpo_step_rt(const Heff2Plan& p, cudaStream_t s) {
   const int nst = p.d1 * p.d2;
   const int cpad = (nst * p.wl + 3) & ~3;
-  const size_t smem = sizeof(float) * ((size_t)nst * p.wr * cpad + (size_t)RT_A * cpad * 32);
+  const size_t smem = sizeof(float) * ((size_t)nst * p.wr * cpad + (size_t)RT_A * cpad * 33);
   if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
   static bool attr = false;
   if (!attr) {
