@@ -45,6 +45,8 @@ constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 constexpr int TILE_B_BYTES = BN * BK * 4;   // 16 KB
 constexpr int STAGE_BYTES = 2 * TILE_A_BYTES + 2 * TILE_B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align slack*/ + 256 /*barriers*/;
+// dynamic shared memory of the GEMM for an N-tile width of bnt columns
+constexpr int gemm_smem_bytes(int bnt) { return STAGES * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256; }
 constexpr int GEMM_THREADS = 192;           // 6 warps
 constexpr long long WAIT_CYCLES = 4000000000ll;  // ~2 s at 2 GHz
 
@@ -154,13 +156,16 @@ struct GemmOut {
 // accumulated into its own TMEM buffer (two buffers, double-buffered) and
 // the slice results are summed by the epilogue warps in FP32 registers with
 // ordinary rounding, so the biased part spans at most 32 products.
+template <int BNT>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                        const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
                        int tiles_m, int tiles_n, int group, GemmOut out, int* err) {
+  constexpr int TB_BYTES = BNT * BK * 4;                       // B tile
+  constexpr int ST_BYTES = 2 * TILE_A_BYTES + 2 * TB_BYTES;    // one stage
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* acc_full = empty + STAGES;
   uint64_t* acc_empty = acc_full + NACC;
@@ -177,7 +182,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   const int gsz = min(tiles_m - first_m, group);
   const int local = (int)blockIdx.x - gid * per_group;
   const int m0 = (first_m + local % gsz) * BM;
-  const int n0 = (local / gsz) * BN;
+  const int n0 = (local / gsz) * BNT;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -192,7 +197,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(NACC * BN));
+                 "r"(NACC * BNT));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -206,18 +211,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const int s = kt % STAGES;
         const int it = kt / STAGES;
         if (kt >= STAGES && !mbar_wait(&empty[s], (it - 1) & 1, err)) break;
-        unsigned char* st = smem + s * STAGE_BYTES;
-        mbar_expect_tx(&full[s], STAGE_BYTES);
+        unsigned char* st = smem + s * ST_BYTES;
+        mbar_expect_tx(&full[s], ST_BYTES);
         const int x = kt * BK;
         tma_load_2d(st, &mAhi, &full[s], x, m0);
         tma_load_2d(st + TILE_A_BYTES, &mAlo, &full[s], x, m0);
         tma_load_2d(st + 2 * TILE_A_BYTES, &mBhi, &full[s], x, n0);
-        tma_load_2d(st + 2 * TILE_A_BYTES + TILE_B_BYTES, &mBlo, &full[s], x, n0);
+        tma_load_2d(st + 2 * TILE_A_BYTES + TB_BYTES, &mBlo, &full[s], x, n0);
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_tf32(BM, BN);
+      constexpr uint32_t idesc = idesc_tf32(BM, BNT);
       for (int kt = 0; kt < KT; ++kt) {
         const int s = kt % STAGES;
         const int it = kt / STAGES;
@@ -226,10 +231,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (!mbar_wait(&full[s], it & 1, err)) break;
         if (kt >= NACC && !mbar_wait(&acc_empty[b], (u - 1) & 1, err)) break;
         tc_fence_after();
-        const uint32_t d = tmem + b * BN;
-        const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+        const uint32_t d = tmem + b * BNT;
+        const uint32_t base = smem_u32(smem + s * ST_BYTES);
         const uint32_t ahi = base, alo = base + TILE_A_BYTES;
-        const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TILE_B_BYTES;
+        const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TB_BYTES;
 #pragma unroll
         for (int kk = 0; kk < BK / 8; ++kk) {
           const uint32_t o = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
@@ -247,9 +252,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4); one row per thread
     const int q = warp & 3;
     const int row = q * 32 + lane;
-    float acc[BN];
+    float acc[BNT];
 #pragma unroll
-    for (int c = 0; c < BN; ++c) acc[c] = 0.f;
+    for (int c = 0; c < BNT; ++c) acc[c] = 0.f;
     bool ok = true;
     for (int kt = 0; kt < KT && ok; ++kt) {
       const int b = kt % NACC;
@@ -258,9 +263,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       tc_fence_after();
       if (ok) {
 #pragma unroll
-        for (int c = 0; c < BN; c += 16) {
+        for (int c = 0; c < BNT; c += 16) {
           float v[16];
-          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BN + c, v);
+          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
 #pragma unroll
           for (int j = 0; j < 16; ++j) acc[c + j] += v[j];
         }
@@ -273,13 +278,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // full-width tiles of row-contiguous outputs are written with 16-byte
     // stores (4 floats / 2+2 doubles per step) instead of one element
     const bool inrow = ok && gm < out.M;
-    const bool vec = inrow && out.ldn == 1 && n0 + BN <= out.N &&
+    const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
                      ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
                      (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
     if (inrow) {
       const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
-      for (int c = 0; c < BN; c += 4) {
+      for (int c = 0; c < BNT; c += 4) {
         const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
         const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
         if (vec) {
@@ -325,7 +330,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BN));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BNT));
   }
 }
 
@@ -556,7 +561,6 @@ int make_map(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) 
   return r == CUDA_SUCCESS ? DMRG_OK : DMRG_ERR_ARG;
 }
 
-bool g_attr_set = false;
 
 // C (M x N) = A (M x Kp) . B (N x Kp)^T from split operands.
 // ---------------------------------------------------------------- tile-order tuner
@@ -573,6 +577,7 @@ struct TuneKey {
   }
 };
 struct TuneVal {
+  int bnt;
   int group;
   float ms;
 };
@@ -586,78 +591,104 @@ TuneKey tune_key(int M, int N, int K) {
   return TuneKey{dev, M, N, K};
 }
 bool tune_enabled() { return g_tune_on.load() != 0; }
-bool tune_lookup(const TuneKey& k, int* group) {
+struct GemmCfg;
+bool tune_lookup(const TuneKey& k, GemmCfg* cfg);
+void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms);
+
+// Launch configuration of one split GEMM: N-tile width (128 or 64 columns)
+// and grouped tile order.
+struct GemmCfg {
+  int bnt;
+  int group;
+};
+
+bool tune_lookup(const TuneKey& k, GemmCfg* cfg) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tune.find(k);
   if (it == g_tune.end()) return false;
-  *group = it->second.group;
+  *cfg = GemmCfg{it->second.bnt, it->second.group};
   return true;
 }
-void tune_store(const TuneKey& k, int group, float ms) {
+void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_tune[k] = TuneVal{group, ms};
+  g_tune[k] = TuneVal{cfg.bnt, cfg.group, ms};
+}
+
+template <int BNT>
+int gemm_launch(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi, const float* Blo, int M, int N,
+                int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       gemm_smem_bytes(BNT)));
+    attr = true;
+  }
+  CUtensorMap mbh, mbl;
+  DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BNT));
+  DMRG_TRY(make_map(&mbl, Blo, N, Kp, BNT));
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BNT - 1) / BNT;
+  const long long tiles = (long long)tiles_m * tiles_n;
+  if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
+  const int g = group < 1 ? 1 : (group > tiles_m ? tiles_m : group);
+  tf32x3_gemm_kernel<BNT><<<(unsigned)tiles, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
+      mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n, g, out, err);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
 }
 
 int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
                const GemmOut& out, int* err, cudaStream_t s) {
   DMRG_TRY(get_encoder());
-  CUtensorMap mah, mal, mbh, mbl;
+  CUtensorMap mah, mal;
   DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM));
   DMRG_TRY(make_map(&mal, Alo, M, Kp, BM));
-  DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BN));
-  DMRG_TRY(make_map(&mbl, Blo, N, Kp, BN));
-  if (!g_attr_set) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    g_attr_set = true;
-  }
-  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
-  const long long tiles = (long long)tiles_m * tiles_n;
-  if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
-  auto launch = [&](int group) -> int {
-    tf32x3_gemm_kernel<<<(unsigned)tiles, GEMM_THREADS, SMEM_BYTES, s>>>(mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n,
-                                                                         group, out, err);
-    DMRG_CHECK_LAUNCH();
-    return DMRG_OK;
+  auto launch = [&](const GemmCfg& c) -> int {
+    return c.bnt == 64 ? gemm_launch<64>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
+                       : gemm_launch<128>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
   };
-  int group = tiles_m;
-  // Tile order is tuned per GEMM shape on its first overwrite-mode call
-  // (re-running an overwrite GEMM reproduces its output bit for bit: every
-  // tile sums the same K slices in the same order whatever the order of the
-  // tiles); accumulate-mode calls use the decision for their shape if one
-  // exists, else the plain order.
+  const int tiles_m = (M + BM - 1) / BM;
+  GemmCfg cfg{128, tiles_m};
+  // Tile width and order are tuned per GEMM shape on its first
+  // overwrite-mode call (re-running an overwrite GEMM reproduces its output
+  // bit for bit: every output element sums the same K slices in the same
+  // order whatever the tiling); accumulate-mode calls use the decision for
+  // their shape if one exists, else 128-wide tiles in plain order.
   const TuneKey key = tune_key(M, N, Kp);
-  if (!tune_lookup(key, &group)) {
-    group = tiles_m;
+  if (!tune_lookup(key, &cfg)) {
+    cfg = GemmCfg{128, tiles_m};
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     DMRG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
-    if (tune_enabled() && !out.accumulate && cap == cudaStreamCaptureStatusNone && tiles >= 2 * 152) {
-      const int cand[4] = {tiles_m, 16, 8, 4};
+    const long long tiles128 = (long long)tiles_m * ((N + 127) / 128);
+    if (tune_enabled() && !out.accumulate && cap == cudaStreamCaptureStatusNone && tiles128 >= 48) {
+      const GemmCfg cand[6] = {{128, tiles_m}, {128, 16}, {128, 8}, {64, tiles_m}, {64, 16}, {64, 8}};
       float best = 0.f;
+      bool have = false;
       cudaEvent_t e0, e1;
       DMRG_CUDA_TRY(cudaEventCreate(&e0));
       DMRG_CUDA_TRY(cudaEventCreate(&e1));
-      for (int i = 0; i < 4; ++i) {
-        const int g = cand[i] < tiles_m ? cand[i] : tiles_m;
-        if (i > 0 && g == tiles_m) continue;
-        DMRG_TRY(launch(g));  // warm
+      for (int i = 0; i < 6; ++i) {
+        GemmCfg c = cand[i];
+        if (c.group > tiles_m) c.group = tiles_m;
+        if (i % 3 != 0 && c.group == tiles_m) continue;   // same as the plain order
+        DMRG_TRY(launch(c));  // warm
         DMRG_CUDA_TRY(cudaEventRecord(e0, s));
-        DMRG_TRY(launch(g));
+        DMRG_TRY(launch(c));
         DMRG_CUDA_TRY(cudaEventRecord(e1, s));
         DMRG_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0.f;
         DMRG_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-        if (i == 0 || ms < best) {
+        if (!have || ms < best) {
           best = ms;
-          group = g;
+          cfg = c;
+          have = true;
         }
       }
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
-      tune_store(key, group, best);
-      return launch(group);
+      tune_store(key, cfg, best);
     }
   }
-  return launch(group);
+  return launch(cfg);
 }
 
 int split_rows(const double* in, long long ldr, long long ldk, int R, int K, int Kp, float* hi, float* lo,
@@ -1090,12 +1121,13 @@ extern "C" int dmrg_autotune_entries(int* out, int max_entries) {
   int n = 0;
   for (const auto& kv : dmrg::g_tune) {
     if (out && n < max_entries) {
-      int* e = out + 5 * n;
+      int* e = out + 6 * n;
       e[0] = kv.first.M;
       e[1] = kv.first.N;
       e[2] = kv.first.K;
-      e[3] = kv.second.group;
-      e[4] = (int)(kv.second.ms * 1000.f);
+      e[3] = kv.second.bnt;
+      e[4] = kv.second.group;
+      e[5] = (int)(kv.second.ms * 1000.f);
     }
     ++n;
   }

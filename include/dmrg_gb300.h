@@ -224,19 +224,21 @@ int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* s
                            int iters, void* left_out, void* right_out, double* discarded,
                            void* work, size_t work_bytes, void* stream);
 
-/* ---- tile-order autotuner of the split-TF32 GEMM -------------------------
- * The tensor-core GEMM walks its output tiles in groups of `group` M-tiles
- * per N-tile; on the first overwrite-mode call of each shape (M, N, K) on a
- * device the library times the plain order and groups of 16, 8 and 4 and
- * keeps the fastest.  The shapes of a sweep are functions of
- * (chi_left, chi_right, d, w), so the decisions are effectively keyed on
- * those.  Results do not depend on the order (every tile sums the same K
- * slices in the same order).  No reference counterpart (the reference's
- * contraction order is chosen per call in Python, pyitensor/kernels.py:298-334). */
+/* ---- tile autotuner of the split-TF32 GEMM ------------------------------
+ * The tensor-core GEMM uses 128 x 128 or 128 x 64 output tiles and walks
+ * them in groups of `group` M-tiles per N-tile; on the first overwrite-mode
+ * call of each shape (M, N, K) on a device the library times both widths in
+ * plain order and in groups of 16 and 8 and keeps the fastest.  The shapes
+ * of a sweep are functions of (chi_left, chi_right, d, w), so the decisions
+ * are effectively keyed on those.  Results do not depend on the choice
+ * (every output element sums the same K slices in the same order).  No
+ * reference counterpart (the reference's contraction order is chosen per
+ * call in Python, pyitensor/kernels.py:298-334). */
 /* Turn tuning of new shapes on (1, the default) or off; returns the previous setting. */
 int dmrg_autotune_enable(int enable);
-/* Copies up to max_entries decisions as 5 ints each (M, N, K, group, best
- * time in microseconds) into out (may be NULL); returns the number held. */
+/* Copies up to max_entries decisions as 6 ints each (M, N, K, tile width,
+ * group, best time in microseconds) into out (may be NULL); returns the
+ * number held. */
 int dmrg_autotune_entries(int* out, int max_entries);
 
 /* ---- many independent chains at once (FP64 / complex FP64) ----------------
