@@ -37,14 +37,11 @@ namespace dmrg {
 namespace {
 
 constexpr int BM = 128;     // accumulator rows = TMEM lanes
-constexpr int BN = 128;     // accumulator columns (fp32) per TMEM buffer
+constexpr int BN = 128;     // widest N tile: accumulator columns (fp32) per TMEM buffer
 constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
 constexpr int STAGES = 3;
 constexpr int NACC = 2;     // TMEM accumulator buffers (one K-slice each)
 constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
-constexpr int TILE_B_BYTES = BN * BK * 4;   // 16 KB
-constexpr int STAGE_BYTES = 2 * TILE_A_BYTES + 2 * TILE_B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align slack*/ + 256 /*barriers*/;
 // dynamic shared memory of the GEMM for an N-tile width of bnt columns
 constexpr int gemm_smem_bytes(int bnt) { return STAGES * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256; }
 constexpr int GEMM_THREADS = 192;           // 6 warps
@@ -871,6 +868,22 @@ int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, con
   else DMRG_TRY(split_transpose(B, ldb, k, n, Kp, bhi, blo, s));
   GemmOut g{C, ldc, 1, m, n, 1, accumulate, alpha};
   return gemm_split(ahi, alo, bhi, blo, m, n, Kp, g, err, s);
+}
+
+// Products of a matrix with itself, splitting it once (one operand table
+// serves both sides of the GEMM):
+//   gram = 1: C (k x k) = alpha X^T X with X (inner x k, ld);
+//   gram = 0: C (k x k) = alpha X X   with X (k x k, ld) symmetric.
+int tf32x3_gemm_self(int gram, int k, int inner, float alpha, const double* X, long long ld, int accumulate,
+                     double* C, long long ldc, void* work, int* err, cudaStream_t s) {
+  const int Kp = pad32(inner);
+  char* b = static_cast<char*>(work) + align_up(256, 1024);
+  float* hi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)k * Kp, 1024);
+  float* lo = reinterpret_cast<float*>(b);
+  if (gram) DMRG_TRY(split_transpose(X, ld, inner, k, Kp, hi, lo, s));
+  else DMRG_TRY(split_rows(X, ld, 1, k, inner, Kp, hi, lo, s));
+  GemmOut g{C, ldc, 1, k, k, 1, accumulate, alpha};
+  return gemm_split(hi, lo, hi, lo, k, k, Kp, g, err, s);
 }
 
 // ---------------------------------------------------------------- plain GEMM (merges)

@@ -24,6 +24,11 @@ int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, con
                    const double* B, long long ldb, int accumulate, double* C, long long ldc, void* work, int* err,
                    cudaStream_t s);
 
+// C (k x k) (+)= alpha X^T X (gram = 1, X inner x k) or alpha X X (gram = 0,
+// X k x k symmetric), splitting X once; same workspace as tf32x3_gemm_ex
+int tf32x3_gemm_self(int gram, int k, int inner, float alpha, const double* X, long long ld, int accumulate,
+                     double* C, long long ldc, void* work, int* err, cudaStream_t s);
+
 // warm-started subspace-iteration truncation (subspace.cu)
 size_t subspace_workspace_bytes(int m, int n, int k);
 int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,

@@ -437,7 +437,13 @@ class Engine:
                 start = Ai.reshape(m, Ai.shape[2])
                 kx = min(start.shape[1], rank)
                 start = start[:, :kx].contiguous()
-            lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb)
+            try:
+                lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb)
+            except _lib.DmrgError as ex:
+                if ex.status != _lib.DMRG_ERR_NOCONV:
+                    raise
+                # the polar iteration did not converge: exact FP64 truncation
+                lo, ro, s, keep, disc = self.svd(theta.view(m, n), 0.0, rank, 1, absorb)
         else:
             lo, ro, s, keep, disc = self.svd(theta.view(m, n), cutoff, maxdim, 1, absorb)
         t3 = time.perf_counter()
