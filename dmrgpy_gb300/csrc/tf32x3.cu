@@ -37,7 +37,6 @@ namespace dmrg {
 namespace {
 
 constexpr int BM = 128;     // accumulator rows = TMEM lanes
-constexpr int BN = 128;     // widest N tile: accumulator columns (fp32) per TMEM buffer
 constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
 constexpr int STAGES = 3;
 constexpr int NACC = 2;     // TMEM accumulator buffers (one K-slice each)
