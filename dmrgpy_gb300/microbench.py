@@ -66,10 +66,12 @@ def main(argv=None):
     elif args.op == "subspace":
         m = chi * d
         M2 = theta.reshape(m, m)
-        start = torch.linalg.qr(rnd(m, chi))[0].contiguous()
 
+        # no warm start: the library draws and orthonormalises the start
+        # basis itself (the first sweep's case; warm-started calls in a
+        # converged sweep skip that orthonormalisation)
         def call():
-            eng.subspace_split(M2, chi, start, chi, 0)
+            eng.subspace_split(M2, chi, None, 0, 0)
         flops = 2.0 * 3 * m * m * chi
     elif args.op == "svd":
         m = chi * d
