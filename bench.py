@@ -227,15 +227,11 @@ def run_gpu(args):
     # the NVTX range lets a profiler restrict itself to the timed sweeps
     # (ncu --nvtx --nvtx-include "timed_sweeps/")
     torch.cuda.nvtx.range_push("timed_sweeps")
-    # the NVTX range lets a profiler restrict itself to the timed sweeps
-    # (ncu --nvtx --nvtx-include "timed_sweeps/")
-    torch.cuda.nvtx.range_push("timed_sweeps")
     ev0.record()
     energy = None
     for _ in range(args.steps):
         energy = eng.sweep(A, CHI, 0.0, 2, record=True)
     ev1.record()
-    torch.cuda.nvtx.range_pop()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
