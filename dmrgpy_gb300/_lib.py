@@ -27,6 +27,8 @@ REAL64 = 0
 COMPLEX128 = 1
 PREC_FP64 = 0
 PREC_TF32X3 = 1
+GRAM_FP64 = 0
+GRAM_DIGITS = 1
 
 c_size_t = ctypes.c_size_t
 c_int = ctypes.c_int
@@ -81,6 +83,8 @@ SIGNATURES = [
     ("dmrg_subspace_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
     ("dmrg_subspace_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p,
                                        c_void_p, P_double, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_gram_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
+    ("dmrg_gram", c_int, [c_int, c_int, c_int, c_void_p, ctypes.c_longlong, c_void_p, c_void_p, c_size_t, c_void_p]),
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),

@@ -607,6 +607,33 @@ int dmrg_gemm(int dtype, int precision, int m, int k, int n, const void* A, cons
                        static_cast<double*>(C), s);
 }
 
+size_t dmrg_gram_workspace_bytes(int method, int m, int k) {
+  if (m <= 0 || k <= 0) return 0;
+  return method == DMRG_GRAM_DIGITS ? gram_digits_workspace_bytes(m, k) : 0;
+}
+
+int dmrg_gram(int method, int m, int k, const void* X, long long ld, void* G, void* work, size_t work_bytes,
+              void* stream) {
+  if (m <= 0 || k <= 0 || ld < k || !X || !G) return DMRG_ERR_ARG;
+  if (method != DMRG_GRAM_FP64 && method != DMRG_GRAM_DIGITS) return DMRG_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const double* x = static_cast<const double*>(X);
+  double* g = static_cast<double*>(G);
+  if (method == DMRG_GRAM_FP64) {
+    DMRG_TRY(tgemm_gram(x, ld, m, k, g, s));
+    DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+    return DMRG_OK;
+  }
+  if (!work || dmrg_gram_workspace_bytes(method, m, k) > work_bytes) return DMRG_ERR_WORKSPACE;
+  int* err = static_cast<int*>(work);   // the workspace head is reserved for the status word
+  DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  DMRG_TRY(gram_digits(x, ld, m, k, g, work, work_bytes, err, s));
+  int h = 0;
+  DMRG_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  return h;
+}
+
 size_t dmrg_subspace_workspace_bytes(int m, int n, int k) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
   return subspace_workspace_bytes(m, n, k);

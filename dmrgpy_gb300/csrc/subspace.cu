@@ -1,7 +1,8 @@
 // Truncation of a two-site tensor by warm-started subspace iteration, for
 // the split-TF32 sweep at large bond dimension when the kept dimension is
 // fixed by maxdim (cutoff <= 0): no eigensolver, only GEMMs on the tensor
-// cores plus one FP64 Gram matrix.
+// cores, one of them a Gram matrix accurate to ~1e-13 (exact digit products,
+// gram.cu).
 //
 //   keep the left factor (absorb 0):
 //     Y = theta^T X      X: m x k start basis (the current left site tensor)
@@ -14,9 +15,9 @@
 //
 // orth() is the polar factor of the block by Newton-Schulz iterations, which
 // are GEMMs only (split-TF32 on the tensor cores); the final left/right basis
-// gets one more correction from an FP64 Gram matrix so that it is orthonormal
-// to ~1e-11 (a basis that is only FP32-orthonormal lets the norm environment
-// drift along the chain).
+// gets one more correction from a near-FP64 Gram matrix so that it is
+// orthonormal to ~1e-11 (a basis that is only FP32-orthonormal lets the norm
+// environment drift along the chain).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -191,13 +192,19 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
 // The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
 // what a product accurate to ~5e-7 can resolve.  A left basis that is only
 // that orthonormal makes the norm environment drift by ~N x 1e-6 over a
-// chain, so a kept basis gets one correction with an FP64 Gram:
-//   E = X^T X - I (FP64),  X <- X (I - E/2)   (residual O(E^2)),
+// chain, so a kept basis gets one correction with a Gram matrix from exact
+// digit products (~1e-13, gram.cu; the FP64 CUDA-core Gram beyond its size
+// limit):
+//   E = X^T X - I,  X <- X (I - E/2)   (residual O(E^2)),
 // where the product X (E/2) only needs the split-TF32 relative accuracy
 // because E is already tiny.
 int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* B, unsigned long long* dev, void* gw,
-                      int* err, cudaStream_t s) {
-  DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
+                      size_t gw_bytes, int* err, cudaStream_t s) {
+  // the Gram from exact digit products on the tensor cores; the FP64
+  // CUDA-core Gram beyond its size limit
+  const int st = gram_digits(Z, ld, m, k, A, gw, gw_bytes, err, s);
+  if (st == DMRG_ERR_ARG || st == DMRG_ERR_WORKSPACE) DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
+  else DMRG_TRY(st);
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
   poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
   DMRG_CHECK_LAUNCH();
@@ -217,13 +224,13 @@ int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, d
 }
 
 int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
-               unsigned long long* dev, void* gw, int* err, bool exact, cudaStream_t s) {
+               unsigned long long* dev, void* gw, size_t gw_bytes, int* err, bool exact, cudaStream_t s) {
   // an input that is already orthonormal (the usual warm start) skips the
   // iterations
   double d0 = 1.0;
   DMRG_TRY(tf32x3_gemm_self(1, k, m, 1.f, Z, ld, 0, A, k, gw, err, s));
   DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
-  if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, err, s) : DMRG_OK;
+  if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s) : DMRG_OK;
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
   colsq_kernel<<<(k + 255) / 256, 256, 0, s>>>(Z, ld, m, k, n2);
   DMRG_CHECK_LAUNCH();
@@ -271,18 +278,25 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   // level) is reported instead of being corrected: the caller falls back to
   // the FP64 SVD
   if (!(d < 1e-3)) return DMRG_ERR_NOCONV;
-  if (exact) DMRG_TRY(orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, err, s));
+  if (exact) DMRG_TRY(orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s));
   return DMRG_OK;
 }
 
 }  // namespace
+
+// scratch shared by the split-TF32 GEMMs and the digit Gram
+size_t gemm_scratch_bytes(int big) {
+  const size_t a = tf32x3_gemm_ex_workspace_bytes(big, big, big);
+  const size_t b = gram_digits_workspace_bytes(big, big);
+  return a > b ? a : b;
+}
 
 size_t subspace_workspace_bytes(int m, int n, int k) {
   const size_t big = (size_t)(m > n ? m : n);
   const size_t d = sizeof(double);
   return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 5 * align_up(d * big * k, 1024) +
          2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) +
-         tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big) + align_up(64, 1024);
+         gemm_scratch_bytes((int)big) + align_up(64, 1024);
 }
 
 // theta (m x n row-major).  absorb 0 keeps an orthonormal LEFT basis; X is
@@ -314,13 +328,15 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   double* PA = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* PB_ = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* Pn2 = reinterpret_cast<double*>(p); p += align_up(d * k, 1024);
-  void* gw = p; p += tf32x3_gemm_ex_workspace_bytes((int)big, (int)big, (int)big);
+  void* gw = p;
+  const size_t gw_bytes = gemm_scratch_bytes((int)big);
+  p += gw_bytes;
   double* acc = reinterpret_cast<double*>(p);
   unsigned long long* pdev = reinterpret_cast<unsigned long long*>(acc + 4);
   DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, 256, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(acc, 0, 64, s));
   auto orth = [&](double* Zp, int rows, bool exact) -> int {
-    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, err, exact, s);
+    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, gw_bytes, err, exact, s);
   };
 
   // canonical problem: keep the left basis of Th (M x N); W (N x k) is an

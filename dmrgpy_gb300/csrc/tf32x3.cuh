@@ -29,6 +29,13 @@ int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, con
 int tf32x3_gemm_self(int gram, int k, int inner, float alpha, const double* X, long long ld, int accumulate,
                      double* C, long long ldc, void* work, int* err, cudaStream_t s);
 
+// G (k x k, ld k) = X^T X for X (m x k, ld) with FP64-level accuracy from
+// exact digit products on the tensor cores (gram.cu); m <= 32768
+size_t gram_digits_workspace_bytes(int m, int k);
+int gram_digits(const double* X, long long ld, int m, int k, double* G, void* work, size_t work_bytes, int* err,
+                cudaStream_t s);
+int tgemm_gram(const double* X, long long ld, int m, int k, double* G, cudaStream_t stream);
+
 // warm-started subspace-iteration truncation (subspace.cu)
 size_t subspace_workspace_bytes(int m, int n, int k);
 int subspace_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,

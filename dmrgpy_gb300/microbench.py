@@ -5,7 +5,9 @@
 Ops: heff2 (two-site H_eff matvec, per Krylov iteration: prepared operands),
 env (left environment extension), subspace (fixed-rank truncation of a
 (chi d) x (d chi) two-site tensor), svd (FP64 one-sided Jacobi truncation),
-merge (two-site merge GEMM).  Prints one JSON line with the mean time per
+merge (two-site merge GEMM), gram / gram64 (X^T X of a (chi d) x chi
+block by exact digit products on the tensor cores / in FP64 on the CUDA
+cores).  Prints one JSON line with the mean time per
 call (CUDA events on the launching stream, after warm-up) and the
 algorithmic FLOP rate.  Used to pick bond dimensions and to give profilers a
 small, self-contained target.
@@ -26,7 +28,7 @@ def _heisenberg(n):
 def main(argv=None):
     import torch
     ap = argparse.ArgumentParser()
-    ap.add_argument("--op", default="heff2", choices=["heff2", "env", "subspace", "svd", "merge"])
+    ap.add_argument("--op", default="heff2", choices=["heff2", "env", "subspace", "svd", "merge", "gram", "gram64"])
     ap.add_argument("--chi", type=int, default=1024)
     ap.add_argument("--d", type=int, default=3)
     ap.add_argument("--precision", default="tf32x3", choices=["fp64", "tf32x3"])
@@ -73,6 +75,18 @@ def main(argv=None):
         def call():
             eng.subspace_split(M2, chi, None, 0, 0)
         flops = 2.0 * 3 * m * m * chi
+    elif args.op in ("gram", "gram64"):
+        m = chi * d
+        X = rnd(m, chi)
+        G = torch.empty((chi, chi), dtype=torch.float64, device=dev)
+        method = _lib.GRAM_DIGITS if args.op == "gram" else _lib.GRAM_FP64
+        need = eng.lib.dmrg_gram_workspace_bytes(method, m, chi)
+        gptr, gsize = eng.ws.get(max(need, 1))
+
+        def call():
+            _lib.check("dmrg_gram", eng.lib.dmrg_gram(method, m, chi, X.data_ptr(), chi, G.data_ptr(), gptr,
+                                                      gsize, eng.stream))
+        flops = 1.0 * m * chi * chi   # the symmetric half
     elif args.op == "svd":
         m = chi * d
         M2 = theta.reshape(m, m)

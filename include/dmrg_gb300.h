@@ -280,6 +280,23 @@ int dmrg_batch_svd_factor(int dtype, int nprob, const int* m, const int* n, cons
 int dmrg_batch_svd_output(int dtype, int nprob, const int* m, const int* n, const int* keep, int absorb,
                           void* const* left, void* const* right, void* work, size_t work_bytes, void* stream);
 
+/* ---- Gram matrix ------------------------------------------------------------
+ * No counterpart in the reference (its truncation is an SVD,
+ * pyitensor/svd.py:32-68): G (k x k, row-major) = X^T X for a real FP64
+ * block X (m x k, row-major, leading dimension ld >= k), the orthonormality
+ * check of the subspace truncation.  method DMRG_GRAM_FP64: FP64 on the
+ * CUDA cores (no workspace); DMRG_GRAM_DIGITS: exact digit products on the
+ * tensor cores (columns scaled by powers of two, three 8-bit integer digits
+ * multiplied and summed exactly, the 2^-24 tail in FP32), error ~1e-13
+ * relative to |x_a| |x_b|, m <= 32768 (DMRG_ERR_ARG beyond).  G is exactly
+ * symmetric.  A non-finite entry of X gives DMRG_ERR_NAN (digit method).
+ * Synchronises the stream. */
+#define DMRG_GRAM_FP64 0
+#define DMRG_GRAM_DIGITS 1
+size_t dmrg_gram_workspace_bytes(int method, int m, int k);
+int dmrg_gram(int method, int m, int k, const void* X, long long ld, void* G, void* work, size_t work_bytes,
+              void* stream);
+
 /* ---- dense contraction ---------------------------------------------------- */
 size_t dmrg_gemm_workspace_bytes(int dtype, int precision, int m, int k, int n);
 /* C (m x n) = A (m x k) . B (k x n), all row-major.  Used for the two-site
