@@ -189,6 +189,80 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
   }
 }
 
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// B = b*A + c*I (k x k) stored as the TF32 hi/lo operand pair [r][Kk] of the
+// next GEMM; also reports max|A - I| into *dev
+__global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, float* __restrict__ hi,
+                                  float* __restrict__ lo, int Kk, unsigned long long* __restrict__ dev) {
+  const long long total = (long long)k * k;
+  double mx = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / k), cc = (int)(i % k);
+    const double a = A[i];
+    const double v = b * a + (r == cc ? c : 0.0);
+    const float h = tf32_rn(static_cast<float>(v));
+    hi[(long long)r * Kk + cc] = h;
+    lo[(long long)r * Kk + cc] = tf32_rn(static_cast<float>(v - static_cast<double>(h)));
+    mx = fmax(mx, fabs(a - (r == cc ? 1.0 : 0.0)));
+  }
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    atomicMax(dev, __double_as_longlong(m));
+  }
+}
+
+inline int pad32s(long long x) { return (int)((x + 31) / 32 * 32); }
+
+// TF32 hi/lo operand arrays of the polar iteration (fp32 [rows][K]):
+//   xt  X^T [k][Km]  both operands of the Gram X^T X (K = m)
+//   xr  X   [m][Kk]  A operand of X B (K = k); two of them, because the
+//                    GEMM that reads one writes the next iterate's split
+//   as  A   [k][Kk]  both operands of A A
+//   bs  B   [k][Kk]  B operand of X B (B is symmetric)
+// Each GEMM epilogue writes the splits the next GEMM reads, so the
+// iteration runs without separate split kernels.
+struct PolarSplits {
+  float *xt_hi, *xt_lo, *xr_hi[2], *xr_lo[2], *as_hi, *as_lo, *bs_hi, *bs_lo;
+};
+
+size_t polar_split_bytes(int m, int k) {
+  const size_t Km = pad32s(m), Kk = pad32s(k), f = sizeof(float);
+  return 2 * align_up(f * k * Km, 1024) + 4 * align_up(f * m * Kk, 1024) + 4 * align_up(f * k * Kk, 1024);
+}
+
+PolarSplits polar_splits(void* base, int m, int k) {
+  const size_t Km = pad32s(m), Kk = pad32s(k), f = sizeof(float);
+  char* p = static_cast<char*>(base);
+  auto take = [&](size_t n) {
+    float* r = reinterpret_cast<float*>(p);
+    p += align_up(f * n, 1024);
+    return r;
+  };
+  PolarSplits ps;
+  ps.xt_hi = take(k * Km);
+  ps.xt_lo = take(k * Km);
+  for (int i = 0; i < 2; ++i) {
+    ps.xr_hi[i] = take(m * Kk);
+    ps.xr_lo[i] = take(m * Kk);
+  }
+  ps.as_hi = take(k * Kk);
+  ps.as_lo = take(k * Kk);
+  ps.bs_hi = take(k * Kk);
+  ps.bs_lo = take(k * Kk);
+  return ps;
+}
+
 // The split-TF32 iterations leave |X^T X - I| at the 1e-6 level, which is
 // what a product accurate to ~5e-7 can resolve.  A left basis that is only
 // that orthonormal makes the norm environment drift by ~N x 1e-6 over a
@@ -224,11 +298,24 @@ int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, d
 }
 
 int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
-               unsigned long long* dev, void* gw, size_t gw_bytes, int* err, bool exact, cudaStream_t s) {
+               unsigned long long* dev, void* gw, size_t gw_bytes, void* splits, int* err, bool exact,
+               cudaStream_t s) {
+  const int Km = pad32s(m), Kk = pad32s(k);
+  const PolarSplits ps = polar_splits(splits, m, k);
+  // the K padding of the split arrays must read as zero
+  if (Km != m || Kk != k) DMRG_CUDA_TRY(cudaMemsetAsync(splits, 0, polar_split_bytes(m, k), s));
+  // A = X^T X (FP64), optionally with its split for A A
+  auto gram = [&](bool with_split) -> int {
+    GemmOut g{};
+    g.C = A; g.ldm = k; g.ldn = 1; g.M = k; g.N = k; g.out_f64 = 1; g.alpha = 1.f;
+    if (with_split) { g.rhi = ps.as_hi; g.rlo = ps.as_lo; g.rld = Kk; }
+    return tf32x3_gemm_split(ps.xt_hi, ps.xt_lo, ps.xt_hi, ps.xt_lo, k, k, Km, g, err, s);
+  };
   // an input that is already orthonormal (the usual warm start) skips the
   // iterations
   double d0 = 1.0;
-  DMRG_TRY(tf32x3_gemm_self(1, k, m, 1.f, Z, ld, 0, A, k, gw, err, s));
+  DMRG_TRY(tf32x3_split_transpose(Z, ld, m, k, Km, ps.xt_hi, ps.xt_lo, s));
+  DMRG_TRY(gram(false));
   DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
   if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s) : DMRG_OK;
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
@@ -238,40 +325,48 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   DMRG_CHECK_LAUNCH();
   perturb_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, 1e-8 / sqrt((double)m), 0x5eed5ull + (unsigned)k);
   DMRG_CHECK_LAUNCH();
+  DMRG_TRY(tf32x3_split_transpose(Z, ld, m, k, Km, ps.xt_hi, ps.xt_lo, s));
+  DMRG_TRY(tf32x3_split_rows(Z, ld, m, k, Kk, ps.xr_hi[0], ps.xr_lo[0], s));
   double* X = Z;
   double* Y = X2;
+  int cur = 0;
   // 14 quintic steps lift a direction from the 1e-8 perturbation level to
   // ~0.3; the cubic steps then converge quadratically
   const int quintic = 14, cubic_max = 16;
   double d = 1.0;
   for (int it = 0; it < quintic + cubic_max; ++it) {
     const bool q = it < quintic;
-    // A = X^T X
-    DMRG_TRY(tf32x3_gemm_self(1, k, m, 1.f, X, ld, 0, A, k, gw, err, s));
-    DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+    DMRG_TRY(gram(q));
+    // Y = X B (+ a X), written with the next iterate's two splits
+    GemmOut xb{};
+    xb.C = Y; xb.ldm = ld; xb.ldn = 1; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = 1.f;
+    xb.rhi = ps.xr_hi[1 - cur]; xb.rlo = ps.xr_lo[1 - cur]; xb.rld = Kk;
+    xb.thi = ps.xt_hi; xb.tlo = ps.xt_lo; xb.tld = Km;
     if (q) {
-      // B = b A + c A^2 ;  X <- a X + X B
+      // B = b A + c A^2 (split only) ;  X <- a X + X B
       const double a = 3.4445, b = -4.7750, c = 2.0315;
-      poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, b, 0.0, B, dev);
-      DMRG_CHECK_LAUNCH();
-      DMRG_TRY(tf32x3_gemm_self(0, k, k, (float)c, A, k, 1, B, k, gw, err, s));
-      // Y = a X ; Y += X B
-      DMRG_TRY(copy_scaled(X, ld, Y, ld, m, k, a, s));
-      DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, X, ld, B, k, 1, Y, ld, gw, err, s));
+      GemmOut b2{};
+      b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)c;
+      b2.cin = A; b2.cin_ld = k; b2.beta = b;
+      b2.rhi = ps.bs_hi; b2.rlo = ps.bs_lo; b2.rld = Kk;
+      DMRG_TRY(tf32x3_gemm_split(ps.as_hi, ps.as_lo, ps.as_hi, ps.as_lo, k, k, Kk, b2, err, s));
+      xb.cin = X; xb.cin_ld = ld; xb.beta = a;
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
-      poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, B, dev);
+      DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, ps.bs_hi, ps.bs_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       unsigned long long h = 0;
       DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
       DMRG_CUDA_TRY(cudaStreamSynchronize(s));
       memcpy(&d, &h, sizeof(d));
       if (d < 5e-6) break;
-      DMRG_TRY(tf32x3_gemm_ex(0, 0, m, k, k, 1.f, X, ld, B, k, 0, Y, ld, gw, err, s));
     }
+    DMRG_TRY(tf32x3_gemm_split(ps.xr_hi[cur], ps.xr_lo[cur], ps.bs_hi, ps.bs_lo, m, k, Kk, xb, err, s));
     double* t = X;
     X = Y;
     Y = t;
+    cur = 1 - cur;
   }
   if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
   // a basis still far from orthonormal (a direction below the perturbation
@@ -296,7 +391,7 @@ size_t subspace_workspace_bytes(int m, int n, int k) {
   const size_t d = sizeof(double);
   return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 5 * align_up(d * big * k, 1024) +
          2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) +
-         gemm_scratch_bytes((int)big) + align_up(64, 1024);
+         gemm_scratch_bytes((int)big) + polar_split_bytes((int)big, k) + align_up(64, 1024);
 }
 
 // theta (m x n row-major).  absorb 0 keeps an orthonormal LEFT basis; X is
@@ -331,12 +426,13 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   void* gw = p;
   const size_t gw_bytes = gemm_scratch_bytes((int)big);
   p += gw_bytes;
+  void* splits = p; p += polar_split_bytes((int)big, k);
   double* acc = reinterpret_cast<double*>(p);
   unsigned long long* pdev = reinterpret_cast<unsigned long long*>(acc + 4);
   DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, 256, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(acc, 0, 64, s));
   auto orth = [&](double* Zp, int rows, bool exact) -> int {
-    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, gw_bytes, err, exact, s);
+    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, gw_bytes, splits, err, exact, s);
   };
 
   // canonical problem: keep the left basis of Th (M x N); W (N x k) is an

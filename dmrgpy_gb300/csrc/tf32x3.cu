@@ -46,21 +46,101 @@ constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 constexpr int gemm_smem_bytes(int bnt) { return STAGES * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256; }
 constexpr int GEMM_THREADS = 192;           // 6 warps
 
-struct GemmOut {
-  void* C;
-  long long ldm, ldn;   // element strides of C
-  int M, N;
-  int out_f64;          // 1: store double, 0: store float
-  int accumulate;       // 1: C += alpha*result, 0: C = alpha*result
-  float alpha;
-};
+__device__ __forceinline__ void split2(double x, float& hi, float& lo) {
+  hi = to_tf32(static_cast<float>(x));
+  lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
+}
+
+// Epilogue of the polar-iteration GEMMs (GemmOut with cin / split outputs /
+// no C): v = alpha*acc + beta*cin (+ C if accumulate), stored to C (FP64)
+// if present and as TF32 hi/lo pairs, row-major and/or transposed.  The
+// transposed pairs are written by consecutive lanes (= consecutive rows)
+// and so coalesce; the row-major ones use 16-byte stores where aligned.
+template <int BNT>
+__device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out, int gm, int n0) {
+  double* C = static_cast<double*>(out.C);
+  const long long crow = (long long)gm * out.ldm;
+  const bool full = n0 + BNT <= out.N;
+  const bool cvec = full && C && out.ldn == 1 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) && out.ldm % 2 == 0;
+  const bool ivec = full && out.cin && ((reinterpret_cast<uintptr_t>(out.cin) & 15) == 0) && out.cin_ld % 2 == 0;
+  const bool rvec = full && out.rhi && ((reinterpret_cast<uintptr_t>(out.rhi) & 15) == 0) &&
+                    ((reinterpret_cast<uintptr_t>(out.rlo) & 15) == 0) && out.rld % 4 == 0;
+#pragma unroll
+  for (int c = 0; c < BNT; c += 4) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = static_cast<double>(out.alpha * acc[c + j]);
+    if (out.cin) {
+      const double* ip = out.cin + (long long)gm * out.cin_ld + n0 + c;
+      if (ivec) {
+        const double2 a = reinterpret_cast<const double2*>(ip)[0], b = reinterpret_cast<const double2*>(ip)[1];
+        v[0] += out.beta * a.x; v[1] += out.beta * a.y; v[2] += out.beta * b.x; v[3] += out.beta * b.y;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (n0 + c + j < out.N) v[j] += out.beta * ip[j];
+      }
+    }
+    if (C) {
+      if (cvec) {
+        double2* p = reinterpret_cast<double2*>(C + crow + n0 + c);
+        if (out.accumulate) {
+          const double2 a = p[0], b = p[1];
+          v[0] += a.x; v[1] += a.y; v[2] += b.x; v[3] += b.y;
+        }
+        p[0] = make_double2(v[0], v[1]);
+        p[1] = make_double2(v[2], v[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int gn = n0 + c + j;
+          if (gn < out.N) {
+            const long long o = crow + (long long)gn * out.ldn;
+            if (out.accumulate) v[j] += C[o];
+            C[o] = v[j];
+          }
+        }
+      }
+    }
+    if (out.rhi || out.thi) {
+      float h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) split2(v[j], h[j], l[j]);
+      if (out.rhi) {
+        float* ph = out.rhi + (long long)gm * out.rld + n0 + c;
+        float* pl = out.rlo + (long long)gm * out.rld + n0 + c;
+        if (rvec) {
+          *reinterpret_cast<float4*>(ph) = make_float4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<float4*>(pl) = make_float4(l[0], l[1], l[2], l[3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (n0 + c + j < out.N) {
+              ph[j] = h[j];
+              pl[j] = l[j];
+            }
+        }
+      }
+      if (out.thi) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int gn = n0 + c + j;
+          if (gn < out.N) {
+            out.thi[(long long)gn * out.tld + gm] = h[j];
+            out.tlo[(long long)gn * out.tld + gm] = l[j];
+          }
+        }
+      }
+    }
+  }
+}
 
 // The tensor-core FP32 accumulation is not round-to-nearest: summed over a
 // long K its error grows linearly.  Each K-slice of 32 is therefore
 // accumulated into its own TMEM buffer (two buffers, double-buffered) and
 // the slice results are summed by the epilogue warps in FP32 registers with
 // ordinary rounding, so the biased part spans at most 32 products.
-template <int BNT>
+template <int BNT, bool EXTRA>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                        const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
@@ -179,6 +259,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
     }
     const int gm = m0 + row;
+    if constexpr (EXTRA) {
+      if (ok && gm < out.M) store_extra<BNT>(acc, out, gm, n0);
+    } else {
     // full-width tiles of row-contiguous outputs are written with 16-byte
     // stores (4 floats / 2+2 doubles per step) instead of one element
     const bool inrow = ok && gm < out.M;
@@ -229,6 +312,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
       }
     }
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -239,10 +323,6 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 }
 
 // ---------------------------------------------------------------- splitting
-__device__ __forceinline__ void split2(double x, float& hi, float& lo) {
-  hi = to_tf32(static_cast<float>(x));
-  lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
-}
 
 // out[r][k] (r < R, k < Kp) = split(in[r*ldr + k*ldk]) for k < K, 0 beyond.
 template <typename Tin>
@@ -512,12 +592,12 @@ void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms) {
   g_tune[k] = TuneVal{cfg.bnt, cfg.group, ms};
 }
 
-template <int BNT>
-int gemm_launch(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi, const float* Blo, int M, int N,
-                int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
+template <int BNT, bool EXTRA>
+int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi, const float* Blo, int M, int N,
+                  int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        gemm_smem_bytes(BNT)));
     attr = true;
   }
@@ -528,7 +608,7 @@ int gemm_launch(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi
   const long long tiles = (long long)tiles_m * tiles_n;
   if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
   const int g = group < 1 ? 1 : (group > tiles_m ? tiles_m : group);
-  tf32x3_gemm_kernel<BNT><<<(unsigned)tiles, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
+  tf32x3_gemm_kernel<BNT, EXTRA><<<(unsigned)tiles, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
       mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n, g, out, err);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
@@ -540,9 +620,14 @@ int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float
   CUtensorMap mah, mal;
   DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM));
   DMRG_TRY(make_map(&mal, Alo, M, Kp, BM));
+  const bool extra = out.cin || out.rhi || out.thi || !out.C;
+  if (extra && !out.out_f64) return DMRG_ERR_ARG;
   auto launch = [&](const GemmCfg& c) -> int {
-    return c.bnt == 64 ? gemm_launch<64>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
-                       : gemm_launch<128>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
+    if (extra)
+      return c.bnt == 64 ? gemm_launch_t<64, true>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
+                         : gemm_launch_t<128, true>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
+    return c.bnt == 64 ? gemm_launch_t<64, false>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
+                       : gemm_launch_t<128, false>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
   };
   const int tiles_m = (M + BM - 1) / BM;
   GemmCfg cfg{128, tiles_m};
@@ -666,6 +751,20 @@ int launch_mpo_step_rt(const Heff2Plan& p, cudaStream_t s) {
 
 }  // namespace
 
+int tf32x3_gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
+                      const GemmOut& out, int* err, cudaStream_t s) {
+  return gemm_split(Ahi, Alo, Bhi, Blo, M, N, Kp, out, err, s);
+}
+
+int tf32x3_split_rows(const double* in, long long ld, int R, int K, int Kp, float* hi, float* lo, cudaStream_t s) {
+  return split_rows(in, ld, 1, R, K, Kp, hi, lo, s);
+}
+
+int tf32x3_split_transpose(const double* in, long long ld, int R, int C, int Rp, float* hi, float* lo,
+                           cudaStream_t s) {
+  return split_transpose(in, ld, R, C, Rp, hi, lo, s);
+}
+
 int tma_map_k32(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) {
   DMRG_TRY(get_encoder());
   return make_map(m, base, rows, Kp, box_rows);
@@ -774,22 +873,6 @@ int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, con
   else DMRG_TRY(split_transpose(B, ldb, k, n, Kp, bhi, blo, s));
   GemmOut g{C, ldc, 1, m, n, 1, accumulate, alpha};
   return gemm_split(ahi, alo, bhi, blo, m, n, Kp, g, err, s);
-}
-
-// Products of a matrix with itself, splitting it once (one operand table
-// serves both sides of the GEMM):
-//   gram = 1: C (k x k) = alpha X^T X with X (inner x k, ld);
-//   gram = 0: C (k x k) = alpha X X   with X (k x k, ld) symmetric.
-int tf32x3_gemm_self(int gram, int k, int inner, float alpha, const double* X, long long ld, int accumulate,
-                     double* C, long long ldc, void* work, int* err, cudaStream_t s) {
-  const int Kp = pad32(inner);
-  char* b = static_cast<char*>(work) + align_up(256, 1024);
-  float* hi = reinterpret_cast<float*>(b); b += align_up(sizeof(float) * (size_t)k * Kp, 1024);
-  float* lo = reinterpret_cast<float*>(b);
-  if (gram) DMRG_TRY(split_transpose(X, ld, inner, k, Kp, hi, lo, s));
-  else DMRG_TRY(split_rows(X, ld, 1, k, inner, Kp, hi, lo, s));
-  GemmOut g{C, ldc, 1, k, k, 1, accumulate, alpha};
-  return gemm_split(hi, lo, hi, lo, k, k, Kp, g, err, s);
 }
 
 // ---------------------------------------------------------------- plain GEMM (merges)

@@ -4,6 +4,41 @@
 
 namespace dmrg {
 
+// Output description of one split-TF32 GEMM C[M,N] = alpha * sum_k A[M,k] B[N,k]
+// (both operands K-major split arrays).  The fields after alpha are optional
+// (zero = unused) and need an FP64 output: the stored value is
+//   v = alpha*acc + beta*cin[row*cin_ld + col] (+ C if accumulate),
+// written to C when C is non-null and as TF32 hi/lo pairs row-major
+// ([row*rld + col]) and/or transposed ([col*tld + row]), which are the
+// operand layouts of the next GEMMs of an iteration.
+struct GemmOut {
+  void* C;
+  long long ldm, ldn;   // element strides of C
+  int M, N;
+  int out_f64;          // 1: store double, 0: store float
+  int accumulate;       // 1: C += alpha*result, 0: C = alpha*result
+  float alpha;
+  const double* cin;
+  long long cin_ld;
+  double beta;
+  float* rhi;
+  float* rlo;
+  long long rld;
+  float* thi;
+  float* tlo;
+  long long tld;
+};
+
+// C (M x N) from split operands A (M x Kp) and B (N x Kp), fp32 [rows][Kp]
+// arrays holding TF32 hi/lo pairs (Kp a multiple of 32, zero beyond K)
+int tf32x3_gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
+                      const GemmOut& out, int* err, cudaStream_t s);
+// hi/lo[r][k] = split(in[r*ld + k]) (k < K, zero up to Kp)
+int tf32x3_split_rows(const double* in, long long ld, int R, int K, int Kp, float* hi, float* lo, cudaStream_t s);
+// hi/lo[c][r] = split(in[r*ld + c]) (r < R, zero up to Rp)
+int tf32x3_split_transpose(const double* in, long long ld, int R, int C, int Rp, float* hi, float* lo,
+                           cudaStream_t s);
+
 size_t tf32x3_heff_workspace_bytes(const dmrg_heff_t& o);
 int tf32x3_heff_apply(const dmrg_heff_t& o, const double* x, double* y, void* work, cudaStream_t s);
 // split L/R and the two-site MPO once per operator; then apply per iteration
@@ -23,11 +58,6 @@ size_t tf32x3_gemm_ex_workspace_bytes(int m, int n, int k);
 int tf32x3_gemm_ex(int transA, int transB, int m, int n, int k, float alpha, const double* A, long long lda,
                    const double* B, long long ldb, int accumulate, double* C, long long ldc, void* work, int* err,
                    cudaStream_t s);
-
-// C (k x k) (+)= alpha X^T X (gram = 1, X inner x k) or alpha X X (gram = 0,
-// X k x k symmetric), splitting X once; same workspace as tf32x3_gemm_ex
-int tf32x3_gemm_self(int gram, int k, int inner, float alpha, const double* X, long long ld, int accumulate,
-                     double* C, long long ldc, void* work, int* err, cudaStream_t s);
 
 // G (k x k, ld k) = X^T X for X (m x k, ld) with FP64-level accuracy from
 // exact digit products on the tensor cores (gram.cu); m <= 32768
