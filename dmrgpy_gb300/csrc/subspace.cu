@@ -143,16 +143,27 @@ __global__ void scale_cols_kernel(double* __restrict__ Z, long long ld, int m, i
   }
 }
 
-// n2[c] = sum_r Z[r][c]^2, one warp per column group
-__global__ void colsq_kernel(const double* __restrict__ Z, long long ld, int m, int k, double* __restrict__ n2) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= k) return;
+// n2[c] = sum_r Z[r][c]^2: one block per 32 columns, 32 row lanes per
+// column (coalesced 256-byte row segments), partial sums combined in shared
+// memory in a fixed order (deterministic)
+__global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ Z, long long ld, int m, int k,
+                                                     double* __restrict__ n2) {
+  __shared__ double sh[32][33];
+  const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int r = 0; r < m; ++r) {
-    const double z = Z[(long long)r * ld + c];
-    s = fma(z, z, s);
+  if (c < k)
+    for (int r = ty; r < m; r += 32) {
+      const double z = Z[(long long)r * ld + c];
+      s = fma(z, z, s);
+    }
+  sh[ty][lane] = s;
+  __syncthreads();
+  if (ty == 0 && c < k) {
+    double t = 0.0;
+    for (int j = 0; j < 32; ++j) t += sh[j][lane];
+    n2[c] = t;
   }
-  n2[c] = s;
 }
 
 // Z += eps * (random), keeps exactly dependent directions from staying at 0
@@ -319,7 +330,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
   if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s) : DMRG_OK;
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
-  colsq_kernel<<<(k + 255) / 256, 256, 0, s>>>(Z, ld, m, k, n2);
+  colsq_kernel<<<(k + 31) / 32, 1024, 0, s>>>(Z, ld, m, k, n2);
   DMRG_CHECK_LAUNCH();
   scale_cols_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, n2, 1.0 / sqrt((double)k));
   DMRG_CHECK_LAUNCH();

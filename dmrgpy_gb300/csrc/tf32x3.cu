@@ -40,7 +40,7 @@ namespace {
 constexpr int BM = 128;     // accumulator rows = TMEM lanes
 constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
 constexpr int STAGES = 3;
-constexpr int NACC = 2;     // TMEM accumulator buffers (one K-slice each)
+constexpr int NACC = 4;     // TMEM accumulator buffers (one K-slice each)
 constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 // dynamic shared memory of the GEMM for an N-tile width of bnt columns
 constexpr int gemm_smem_bytes(int bnt) { return STAGES * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256; }
@@ -137,9 +137,26 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
 
 // The tensor-core FP32 accumulation is not round-to-nearest: summed over a
 // long K its error grows linearly.  Each K-slice of 32 is therefore
-// accumulated into its own TMEM buffer (two buffers, double-buffered) and
+// accumulated into its own TMEM buffer (a ring of NACC buffers) and
 // the slice results are summed by the epilogue warps in FP32 registers with
 // ordinary rounding, so the biased part spans at most 32 products.
+// tile index -> origin in the grouped order: consecutive tile indices walk
+// `group` M-tiles for each N-tile, so the tiles in flight at one time share
+// their operand panels in L2 (group = tiles_m is plain M-fastest order)
+__device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int group, int bnt, int& m0, int& n0) {
+  const int per_group = group * tiles_n;
+  const int gid = t / per_group;
+  const int first_m = gid * group;
+  const int gsz = min(tiles_m - first_m, group);
+  const int local = t - gid * per_group;
+  m0 = (first_m + local % gsz) * BM;
+  n0 = (local / gsz) * bnt;
+}
+
+// Persistent: CTA b computes tiles b, b + gridDim.x, ...  The producer and
+// MMA warps run through the K-slices of consecutive tiles without a break
+// (the stage and TMEM rings continue across tiles), so loading and MMAs of
+// the next tile overlap the epilogue's stores of the current one.
 template <int BNT, bool EXTRA>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
@@ -157,16 +174,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  // grouped tile order on a 1-D grid: consecutive CTAs walk `group` M-tiles
-  // for each N-tile, so the CTAs resident at one time share their operand
-  // panels in L2 (group = tiles_m is plain M-fastest order)
-  const int per_group = group * tiles_n;
-  const int gid = (int)blockIdx.x / per_group;
-  const int first_m = gid * group;
-  const int gsz = min(tiles_m - first_m, group);
-  const int local = (int)blockIdx.x - gid * per_group;
-  const int m0 = (first_m + local % gsz) * BM;
-  const int n0 = (local / gsz) * BNT;
+  const int ntiles = tiles_m * tiles_n;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -191,121 +199,143 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      for (int kt = 0; kt < KT; ++kt) {
-        const int s = kt % STAGES;
-        const int it = kt / STAGES;
-        if (kt >= STAGES && !mbar_wait(&empty[s], (it - 1) & 1, err)) break;
-        unsigned char* st = smem + s * ST_BYTES;
-        mbar_expect_tx(&full[s], ST_BYTES);
-        const int x = kt * BK;
-        tma_load_2d(st, &mAhi, &full[s], x, m0);
-        tma_load_2d(st + TILE_A_BYTES, &mAlo, &full[s], x, m0);
-        tma_load_2d(st + 2 * TILE_A_BYTES, &mBhi, &full[s], x, n0);
-        tma_load_2d(st + 2 * TILE_A_BYTES + TB_BYTES, &mBlo, &full[s], x, n0);
+      long long g = 0;   // K-slice counter over all tiles of this CTA
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int m0, n0;
+        tile_origin(t, tiles_m, tiles_n, group, BNT, m0, n0);
+        for (int kt = 0; kt < KT; ++kt, ++g) {
+          const int s = (int)(g % STAGES);
+          const long long it = g / STAGES;
+          if (g >= STAGES && !mbar_wait(&empty[s], (uint32_t)((it - 1) & 1), err)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = smem + s * ST_BYTES;
+          mbar_expect_tx(&full[s], ST_BYTES);
+          const int x = kt * BK;
+          tma_load_2d(st, &mAhi, &full[s], x, m0);
+          tma_load_2d(st + TILE_A_BYTES, &mAlo, &full[s], x, m0);
+          tma_load_2d(st + 2 * TILE_A_BYTES, &mBhi, &full[s], x, n0);
+          tma_load_2d(st + 2 * TILE_A_BYTES + TB_BYTES, &mBlo, &full[s], x, n0);
+        }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = idesc_tf32(BM, BNT);
-      for (int kt = 0; kt < KT; ++kt) {
-        const int s = kt % STAGES;
-        const int it = kt / STAGES;
-        const int b = kt % NACC;
-        const int u = kt / NACC;
-        if (!mbar_wait(&full[s], it & 1, err)) break;
-        if (kt >= NACC && !mbar_wait(&acc_empty[b], (u - 1) & 1, err)) break;
-        tc_fence_after();
-        const uint32_t d = tmem + b * BNT;
-        const uint32_t base = smem_u32(smem + s * ST_BYTES);
-        const uint32_t ahi = base, alo = base + TILE_A_BYTES;
-        const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TB_BYTES;
+      long long g = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        for (int kt = 0; kt < KT; ++kt, ++g) {
+          const int s = (int)(g % STAGES);
+          const long long it = g / STAGES;
+          const int b = (int)(g % NACC);
+          const long long u = g / NACC;
+          if (!mbar_wait(&full[s], (uint32_t)(it & 1), err) ||
+              (g >= NACC && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), err))) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + b * BNT;
+          const uint32_t base = smem_u32(smem + s * ST_BYTES);
+          const uint32_t ahi = base, alo = base + TILE_A_BYTES;
+          const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TB_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < BK / 8; ++kk) {
-          const uint32_t o = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
-          const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
-          const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
-          mma_tf32(d, dah, dbh, idesc, kk != 0);
-          mma_tf32(d, dah, dbl, idesc, 1u);
-          mma_tf32(d, dal, dbh, idesc, 1u);
+          for (int kk = 0; kk < BK / 8; ++kk) {
+            const uint32_t o = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
+            const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
+            const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
+            mma_tf32(d, dah, dbh, idesc, kk != 0);
+            mma_tf32(d, dah, dbl, idesc, 1u);
+            mma_tf32(d, dal, dbh, idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+          mma_commit(&acc_full[b]);
         }
-        mma_commit(&empty[s]);
-        mma_commit(&acc_full[b]);
       }
     }
   } else {
     // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4); one row per thread
     const int q = warp & 3;
     const int row = q * 32 + lane;
-    float acc[BNT];
-#pragma unroll
-    for (int c = 0; c < BNT; ++c) acc[c] = 0.f;
+    long long g = 0;
     bool ok = true;
-    for (int kt = 0; kt < KT && ok; ++kt) {
-      const int b = kt % NACC;
-      const int u = kt / NACC;
-      ok = mbar_wait(&acc_full[b], u & 1, err);
-      tc_fence_after();
-      if (ok) {
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int m0, n0;
+      tile_origin(t, tiles_m, tiles_n, group, BNT, m0, n0);
+      float acc[BNT];
 #pragma unroll
-        for (int c = 0; c < BNT; c += 16) {
-          float v[16];
-          tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
+      for (int c = 0; c < BNT; ++c) acc[c] = 0.f;
+      for (int kt = 0; kt < KT && ok; ++kt, ++g) {
+        const int b = (int)(g % NACC);
+        const long long u = g / NACC;
+        ok = mbar_wait(&acc_full[b], (uint32_t)(u & 1), err);
+        tc_fence_after();
+        if (ok) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[c + j] += v[j];
-        }
-      }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
-    }
-    const int gm = m0 + row;
-    if constexpr (EXTRA) {
-      if (ok && gm < out.M) store_extra<BNT>(acc, out, gm, n0);
-    } else {
-    // full-width tiles of row-contiguous outputs are written with 16-byte
-    // stores (4 floats / 2+2 doubles per step) instead of one element
-    const bool inrow = ok && gm < out.M;
-    const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
-                     ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
-                     (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
-    if (inrow) {
-      const long long rowoff = (long long)gm * out.ldm;
+          for (int c = 0; c < BNT; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
 #pragma unroll
-      for (int c = 0; c < BNT; c += 4) {
-        const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
-        const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
-        if (vec) {
-          if (out.out_f64) {
-            double2* p = reinterpret_cast<double2*>(static_cast<double*>(out.C) + rowoff + n0 + c);
-            double2 u = make_double2(r0, r1), v = make_double2(r2, r3);
-            if (out.accumulate) {
-              const double2 pu = p[0], pv = p[1];
-              u.x += pu.x; u.y += pu.y; v.x += pv.x; v.y += pv.y;
-            }
-            p[0] = u;
-            p[1] = v;
-          } else {
-            float4* p = reinterpret_cast<float4*>(static_cast<float*>(out.C) + rowoff + n0 + c);
-            float4 u = make_float4(r0, r1, r2, r3);
-            if (out.accumulate) {
-              const float4 o = *p;
-              u.x += o.x; u.y += o.y; u.z += o.z; u.w += o.w;
-            }
-            *p = u;
+            for (int j = 0; j < 16; ++j) acc[c + j] += v[j];
           }
-        } else {
-          const float rr[4] = {r0, r1, r2, r3};
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
+      }
+      if (!ok) break;
+      const int gm = m0 + row;
+      if constexpr (EXTRA) {
+        if (gm < out.M) store_extra<BNT>(acc, out, gm, n0);
+      } else {
+      // full-width tiles of row-contiguous outputs are written with 16-byte
+      // stores (4 floats / 2+2 doubles per step) instead of one element
+      const bool inrow = ok && gm < out.M;
+      const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
+                       ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
+                       (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
+      if (inrow) {
+        const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int gn = n0 + c + j;
-            if (gn < out.N) {
-              const long long o = rowoff + (long long)gn * out.ldn;
-              if (out.out_f64) {
-                double* C = static_cast<double*>(out.C);
-                C[o] = out.accumulate ? C[o] + (double)rr[j] : (double)rr[j];
-              } else {
-                float* C = static_cast<float*>(out.C);
-                C[o] = out.accumulate ? C[o] + rr[j] : rr[j];
+        for (int c = 0; c < BNT; c += 4) {
+          const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
+          const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
+          if (vec) {
+            if (out.out_f64) {
+              double2* p = reinterpret_cast<double2*>(static_cast<double*>(out.C) + rowoff + n0 + c);
+              double2 u = make_double2(r0, r1), v = make_double2(r2, r3);
+              if (out.accumulate) {
+                const double2 pu = p[0], pv = p[1];
+                u.x += pu.x; u.y += pu.y; v.x += pv.x; v.y += pv.y;
+              }
+              p[0] = u;
+              p[1] = v;
+            } else {
+              float4* p = reinterpret_cast<float4*>(static_cast<float*>(out.C) + rowoff + n0 + c);
+              float4 u = make_float4(r0, r1, r2, r3);
+              if (out.accumulate) {
+                const float4 o = *p;
+                u.x += o.x; u.y += o.y; u.z += o.z; u.w += o.w;
+              }
+              *p = u;
+            }
+          } else {
+            const float rr[4] = {r0, r1, r2, r3};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int gn = n0 + c + j;
+              if (gn < out.N) {
+                const long long o = rowoff + (long long)gn * out.ldn;
+                if (out.out_f64) {
+                  double* C = static_cast<double*>(out.C);
+                  C[o] = out.accumulate ? C[o] + (double)rr[j] : (double)rr[j];
+                } else {
+                  float* C = static_cast<float*>(out.C);
+                  C[o] = out.accumulate ? C[o] + rr[j] : rr[j];
+                }
               }
             }
           }
@@ -592,6 +622,21 @@ void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms) {
   g_tune[k] = TuneVal{cfg.bnt, cfg.group, ms};
 }
 
+// multiprocessor count of the current device (cached per device)
+int sm_count() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 0;
+  if (dev < 64) {
+    const int c = cache[dev].load();
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  if (dev < 64) cache[dev].store(n);
+  return n;
+}
+
 template <int BNT, bool EXTRA>
 int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi, const float* Blo, int M, int N,
                   int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
@@ -608,7 +653,11 @@ int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const float* B
   const long long tiles = (long long)tiles_m * tiles_n;
   if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
   const int g = group < 1 ? 1 : (group > tiles_m ? tiles_m : group);
-  tf32x3_gemm_kernel<BNT, EXTRA><<<(unsigned)tiles, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
+  // persistent CTAs: one per SM (the shared-memory stages allow no second)
+  const int nsm = sm_count();
+  if (nsm < 1) return DMRG_ERR_CUDA;
+  const long long grid = tiles < nsm ? tiles : nsm;
+  tf32x3_gemm_kernel<BNT, EXTRA><<<(unsigned)grid, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
       mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n, g, out, err);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
