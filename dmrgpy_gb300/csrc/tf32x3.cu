@@ -275,11 +275,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         tc_fence_after();
         if (ok) {
 #pragma unroll
-          for (int c = 0; c < BNT; c += 16) {
-            float v[16];
-            tmem_ld16(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
+          for (int c = 0; c < BNT; c += 64) {
+            float v[64];
+            tmem_ld64(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[c + j] += v[j];
+            for (int j = 0; j < 64; ++j) acc[c + j] += v[j];
           }
         }
         tc_fence_before();
