@@ -461,57 +461,51 @@ __global__ void __launch_bounds__(256) mpo_step_kernel(const float* __restrict__
   }
 }
 
-// Register-tiled form of the same step: warp al of the CTA owns a' = a0+al,
-// lane owns b = b0+lane; the thread keeps its (s,t,k) input column in
-// registers and reads each MPO row as broadcast float4s from shared memory,
-// so the loop is FMA-bound instead of shared-load-bound (one shared load per
-// four FMAs instead of two per FMA).  MAXC >= (d1 d2 wl) rounded up to 4.
+// Register-tiled form of the same step (d1 d2 wl <= 96): warp al of the CTA
+// owns a' = a0+al, lane owns b = b0+lane; the thread keeps its (s,t,k) input
+// column in registers and reads each MPO row as broadcast float4s from
+// shared memory, so the loop is FMA-bound instead of shared-load-bound (one
+// shared load per four FMAs).  MAXC >= (d1 d2 wl) rounded up to 4.
 constexpr int RT_A = 8;
 
+// It reads X1 transposed, X1T[(a',k)][(s,t,b)] (leading
+// dimension d1 d2 chir), as GEMM1 stores it: a warp covers 32 consecutive b
+// of one a', so each of its d1 d2 wl input loads is one coalesced 128-byte
+// segment and the inputs go straight to registers, without the
+// shared-memory staging that an untransposed X1 needs (it held such a kernel
+// to 3 CTAs per SM, with loads and FMAs in separate phases).  W2 and the
+// input offsets are in shared memory (broadcast reads).
 template <int MAXC>
-__global__ void __launch_bounds__(256) mpo_step_rt_kernel(const float* __restrict__ X1, const float* __restrict__ W2,
-                                                          int chil, int d1, int d2, int chir, int wl, int wr, int Kp,
-                                                          float* __restrict__ hi, float* __restrict__ lo) {
+__global__ void __launch_bounds__(256) mpo_step_t_kernel(const float* __restrict__ X1T, const float* __restrict__ W2,
+                                                         int chil, int d1, int d2, int chir, int wl, int wr, int Kp,
+                                                         float* __restrict__ hi, float* __restrict__ lo) {
   extern __shared__ float4 sm4[];
-  float* sm = reinterpret_cast<float*>(sm4);
+  float* sW = reinterpret_cast<float*>(sm4);
   const int nst = d1 * d2;
   const int in_cols = nst * wl;
   const int out_rows = nst * wr;
   const int cpad = (in_cols + 3) & ~3;
-  float* sW = sm;                        // out_rows x cpad, zero padded
-  float* sX = sW + out_rows * cpad;      // [al][c][33]: row stride 33 keeps the
-                                         // staging stores free of bank conflicts
-  const int b0 = blockIdx.x * 32;
-  const int a0 = blockIdx.y * RT_A;
-  const long long ldx = (long long)chil * wl;
+  int* sOff = reinterpret_cast<int*>(sW + out_rows * cpad);   // MAXC input offsets
+  const long long ldt = (long long)nst * chir;
   for (int i = threadIdx.x; i < out_rows * cpad; i += blockDim.x) {
     const int r = i / cpad, c = i - r * cpad;
     sW[i] = c < in_cols ? W2[r * in_cols + c] : 0.f;
   }
-  const int ncolx = RT_A * wl;
-  for (int i = threadIdx.x; i < nst * 32 * ncolx; i += blockDim.x) {
-    const int col = i % ncolx;
-    const int bl = (i / ncolx) % 32;
-    const int st = i / (ncolx * 32);
-    const int al = col / wl, k = col - al * wl;
-    const int b = b0 + bl, a = a0 + al;
-    float v = 0.f;
-    if (b < chir && a < chil) v = X1[((long long)st * chir + b) * ldx + (long long)a * wl + k];
-    sX[(al * cpad + st * wl + k) * 33 + bl] = v;
-  }
-  for (int i = threadIdx.x; i < RT_A * (cpad - in_cols) * 32; i += blockDim.x) {
-    const int per = (cpad - in_cols) * 32;
-    const int al = i / per, rem = i - al * per;
-    sX[(al * cpad + in_cols + rem / 32) * 33 + (rem & 31)] = 0.f;
+  for (int c = threadIdx.x; c < MAXC; c += blockDim.x) {
+    const int st = c / wl, k = c - (c / wl) * wl;
+    sOff[c] = c < in_cols ? (int)(k * ldt + (long long)st * chir) : -1;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  const int al = threadIdx.x >> 5;
-  const int a = a0 + al, b = b0 + lane;
+  const int a = blockIdx.y * RT_A + (threadIdx.x >> 5), b = blockIdx.x * 32 + lane;
   if (a >= chil || b >= chir) return;
+  const float* base = X1T + (long long)a * wl * ldt + b;
   float x[MAXC];
 #pragma unroll
-  for (int c = 0; c < MAXC; ++c) x[c] = c < cpad ? sX[(al * cpad + c) * 33 + lane] : 0.f;
+  for (int c = 0; c < MAXC; ++c) {
+    const int off = sOff[c];
+    x[c] = off >= 0 ? base[off] : 0.f;
+  }
   for (int r = 0; r < out_rows; ++r) {
     const float4* w4 = reinterpret_cast<const float4*>(sW + r * cpad);
     float acc = 0.f;
@@ -779,24 +773,25 @@ Heff2Plan plan2(const dmrg_heff_t& o, void* work) {
 }
 
 template <int MAXC>
-int launch_mpo_step_rt(const Heff2Plan& p, cudaStream_t s) {
+int launch_mpo_step_t(const Heff2Plan& p, cudaStream_t s) {
   const int nst = p.d1 * p.d2;
   const int cpad = (nst * p.wl + 3) & ~3;
-  const size_t smem = sizeof(float) * ((size_t)nst * p.wr * cpad + (size_t)RT_A * cpad * 33);
+  const size_t smem = sizeof(float) * (size_t)nst * p.wr * cpad + sizeof(int) * MAXC;
   if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
   static bool attr = false;
   if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_rt_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_t_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        200 * 1024));
     attr = true;
   }
   dim3 grid((p.cr + 31) / 32, (p.cl + RT_A - 1) / RT_A);
   if (grid.y > 65535) return DMRG_ERR_ARG;
-  mpo_step_rt_kernel<MAXC><<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi,
-                                                   p.X3_lo);
+  mpo_step_t_kernel<MAXC><<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi,
+                                                  p.X3_lo);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }
+
 
 }  // namespace
 
@@ -849,15 +844,18 @@ int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y,
   Heff2Plan p = plan2(o, work);
   // theta (cl, d1 d2 cr) -> thetaT rows (s,t,b), K = a
   DMRG_TRY(split_transpose(x, p.M1, p.cl, (int)p.M1, p.Kp1, p.thT_hi, p.thT_lo, s));
-  GemmOut g1{p.X1, p.N1, 1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
-  DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
   const int nst = p.d1 * p.d2;
   const int in_cols = nst * p.wl;
-  if (in_cols <= 48) {
-    DMRG_TRY(launch_mpo_step_rt<48>(p, s));
-  } else if (in_cols <= 96) {
-    DMRG_TRY(launch_mpo_step_rt<96>(p, s));
+  if (in_cols <= 96) {
+    // X1 stored transposed, X1T[(a',k)][(s,t,b)]: the epilogue's stores
+    // coalesce across lanes (consecutive rows) and so do the MPO step's loads
+    GemmOut g1{p.X1, 1, p.M1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
+    DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
+    if (in_cols <= 48) DMRG_TRY(launch_mpo_step_t<48>(p, s));
+    else DMRG_TRY(launch_mpo_step_t<96>(p, s));
   } else {
+    GemmOut g1{p.X1, p.N1, 1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
+    DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
     DMRG_TRY(mpo_step_generic(p, s));
   }
   GemmOut g4{y, p.cr, 1, (int)p.M4, p.cr, 1, 0, 1.f};
