@@ -239,17 +239,18 @@ inline int pad32s(long long x) { return (int)((x + 31) / 32 * 32); }
 //   xt  X^T [k][Km]  both operands of the Gram X^T X (K = m)
 //   xr  X   [m][Kk]  A operand of X B (K = k); two of them, because the
 //                    GEMM that reads one writes the next iterate's split
-//   as  A   [k][Kk]  both operands of A A
+//   as  A   [k][Kk]  A operand of A (c A + b I)
+//   ps  c A + b I    B operand of the same product
 //   bs  B   [k][Kk]  B operand of X B (B is symmetric)
 // Each GEMM epilogue writes the splits the next GEMM reads, so the
 // iteration runs without separate split kernels.
 struct PolarSplits {
-  float *xt_hi, *xt_lo, *xr_hi[2], *xr_lo[2], *as_hi, *as_lo, *bs_hi, *bs_lo;
+  float *xt_hi, *xt_lo, *xr_hi[2], *xr_lo[2], *as_hi, *as_lo, *ps_hi, *ps_lo, *bs_hi, *bs_lo;
 };
 
 size_t polar_split_bytes(int m, int k) {
   const size_t Km = pad32s(m), Kk = pad32s(k), f = sizeof(float);
-  return 2 * align_up(f * k * Km, 1024) + 4 * align_up(f * m * Kk, 1024) + 4 * align_up(f * k * Kk, 1024);
+  return 2 * align_up(f * k * Km, 1024) + 4 * align_up(f * m * Kk, 1024) + 6 * align_up(f * k * Kk, 1024);
 }
 
 PolarSplits polar_splits(void* base, int m, int k) {
@@ -269,6 +270,8 @@ PolarSplits polar_splits(void* base, int m, int k) {
   }
   ps.as_hi = take(k * Kk);
   ps.as_lo = take(k * Kk);
+  ps.ps_hi = take(k * Kk);
+  ps.ps_lo = take(k * Kk);
   ps.bs_hi = take(k * Kk);
   ps.bs_lo = take(k * Kk);
   return ps;
@@ -348,20 +351,22 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   for (int it = 0; it < quintic + cubic_max; ++it) {
     const bool q = it < quintic;
     DMRG_TRY(gram(q));
-    // Y = X B (+ a X), written with the next iterate's two splits
+    // Y = X B, written with the next iterate's two splits
     GemmOut xb{};
     xb.C = Y; xb.ldm = ld; xb.ldn = 1; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = 1.f;
     xb.rhi = ps.xr_hi[1 - cur]; xb.rlo = ps.xr_lo[1 - cur]; xb.rld = Kk;
     xb.thi = ps.xt_hi; xb.tlo = ps.xt_lo; xb.tld = Km;
     if (q) {
-      // B = b A + c A^2 (split only) ;  X <- a X + X B
+      // B = a I + A (b I + c A) (split only), so that X <- X B is the quintic
+      // step a X + b X A + c X A^2 as one product
       const double a = 3.4445, b = -4.7750, c = 2.0315;
+      DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
+      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, c, b, ps.ps_hi, ps.ps_lo, Kk, dev);
+      DMRG_CHECK_LAUNCH();
       GemmOut b2{};
-      b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)c;
-      b2.cin = A; b2.cin_ld = k; b2.beta = b;
+      b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = 1.f; b2.diag = a;
       b2.rhi = ps.bs_hi; b2.rlo = ps.bs_lo; b2.rld = Kk;
-      DMRG_TRY(tf32x3_gemm_split(ps.as_hi, ps.as_lo, ps.as_hi, ps.as_lo, k, k, Kk, b2, err, s));
-      xb.cin = X; xb.cin_ld = ld; xb.beta = a;
+      DMRG_TRY(tf32x3_gemm_split(ps.as_hi, ps.as_lo, ps.ps_hi, ps.ps_lo, k, k, Kk, b2, err, s));
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));

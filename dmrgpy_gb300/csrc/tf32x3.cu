@@ -39,11 +39,16 @@ namespace {
 
 constexpr int BM = 128;     // accumulator rows = TMEM lanes
 constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
-constexpr int STAGES = 3;
+// shared-memory stages: 3 x 64 KB for 128-wide tiles, 4 x 48 KB for
+// 64-wide (a stage's TMA round trip is ~2 us under load, so the bytes in
+// flight bound the K-slice rate)
+template <int BNT> __host__ __device__ constexpr int stages_of() { return BNT == 64 ? 4 : 3; }
 constexpr int NACC = 4;     // TMEM accumulator buffers (one K-slice each)
 constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 // dynamic shared memory of the GEMM for an N-tile width of bnt columns
-constexpr int gemm_smem_bytes(int bnt) { return STAGES * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256; }
+constexpr int gemm_smem_bytes(int bnt) {
+  return (bnt == 64 ? 4 : 3) * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256;
+}
 constexpr int GEMM_THREADS = 192;           // 6 warps
 
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
@@ -51,9 +56,11 @@ __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
   lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
 }
 
-// Epilogue of the polar-iteration GEMMs (GemmOut with cin / split outputs /
-// no C): v = alpha*acc + beta*cin (+ C if accumulate), stored to C (FP64)
-// if present and as TF32 hi/lo pairs, row-major and/or transposed.  The
+// Epilogue of the polar-iteration GEMMs (GemmOut with split outputs, a
+// diagonal term or no C): v = alpha*acc + diag*[row == col] (+ C if
+// accumulate), stored to C (FP64) if present and as TF32 hi/lo pairs,
+// row-major and/or transposed.  It only stores (no loads unless it
+// accumulates), so the stores of one tile overlap the next tile's MMAs; the
 // transposed pairs are written by consecutive lanes (= consecutive rows)
 // and so coalesce; the row-major ones use 16-byte stores where aligned.
 template <int BNT>
@@ -62,25 +69,13 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
   const long long crow = (long long)gm * out.ldm;
   const bool full = n0 + BNT <= out.N;
   const bool cvec = full && C && out.ldn == 1 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) && out.ldm % 2 == 0;
-  const bool ivec = full && out.cin && ((reinterpret_cast<uintptr_t>(out.cin) & 15) == 0) && out.cin_ld % 2 == 0;
   const bool rvec = full && out.rhi && ((reinterpret_cast<uintptr_t>(out.rhi) & 15) == 0) &&
                     ((reinterpret_cast<uintptr_t>(out.rlo) & 15) == 0) && out.rld % 4 == 0;
 #pragma unroll
   for (int c = 0; c < BNT; c += 4) {
     double v[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = static_cast<double>(out.alpha * acc[c + j]);
-    if (out.cin) {
-      const double* ip = out.cin + (long long)gm * out.cin_ld + n0 + c;
-      if (ivec) {
-        const double2 a = reinterpret_cast<const double2*>(ip)[0], b = reinterpret_cast<const double2*>(ip)[1];
-        v[0] += out.beta * a.x; v[1] += out.beta * a.y; v[2] += out.beta * b.x; v[3] += out.beta * b.y;
-      } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-          if (n0 + c + j < out.N) v[j] += out.beta * ip[j];
-      }
-    }
+    for (int j = 0; j < 4; ++j) v[j] = static_cast<double>(out.alpha * acc[c + j]) + (n0 + c + j == gm ? out.diag : 0.0);
     if (C) {
       if (cvec) {
         double2* p = reinterpret_cast<double2*>(C + crow + n0 + c);
@@ -164,6 +159,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                        int tiles_m, int tiles_n, int group, GemmOut out, int* err) {
   constexpr int TB_BYTES = BNT * BK * 4;                       // B tile
   constexpr int ST_BYTES = 2 * TILE_A_BYTES + 2 * TB_BYTES;    // one stage
+  constexpr int STAGES = stages_of<BNT>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
@@ -294,10 +290,24 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       // full-width tiles of row-contiguous outputs are written with 16-byte
       // stores (4 floats / 2+2 doubles per step) instead of one element
       const bool inrow = ok && gm < out.M;
+      // transposed FP32 overwrite (the matvec's X1): one coalesced 4-byte
+      // store per element across the warp's consecutive rows, no branches
+      const bool tstore = inrow && out.ldm == 1 && !out.out_f64 && !out.accumulate;
+      if (tstore) {
+        float* pc = static_cast<float*>(out.C) + gm + (long long)n0 * out.ldn;
+        if (n0 + BNT <= out.N) {
+#pragma unroll
+          for (int c = 0; c < BNT; ++c) pc[(long long)c * out.ldn] = out.alpha * acc[c];
+        } else {
+#pragma unroll
+          for (int c = 0; c < BNT; ++c)
+            if (n0 + c < out.N) pc[(long long)c * out.ldn] = out.alpha * acc[c];
+        }
+      }
       const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
                        ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
                        (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
-      if (inrow) {
+      if (inrow && !tstore) {
         const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
         for (int c = 0; c < BNT; c += 4) {
@@ -663,7 +673,7 @@ int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float
   CUtensorMap mah, mal;
   DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM));
   DMRG_TRY(make_map(&mal, Alo, M, Kp, BM));
-  const bool extra = out.cin || out.rhi || out.thi || !out.C;
+  const bool extra = out.rhi || out.thi || !out.C || out.diag != 0.0;
   if (extra && !out.out_f64) return DMRG_ERR_ARG;
   auto launch = [&](const GemmCfg& c) -> int {
     if (extra)

@@ -7,7 +7,7 @@ namespace dmrg {
 // Output description of one split-TF32 GEMM C[M,N] = alpha * sum_k A[M,k] B[N,k]
 // (both operands K-major split arrays).  The fields after alpha are optional
 // (zero = unused) and need an FP64 output: the stored value is
-//   v = alpha*acc + beta*cin[row*cin_ld + col] (+ C if accumulate),
+//   v = alpha*acc + diag*[row == col] (+ C if accumulate),
 // written to C when C is non-null and as TF32 hi/lo pairs row-major
 // ([row*rld + col]) and/or transposed ([col*tld + row]), which are the
 // operand layouts of the next GEMMs of an iteration.
@@ -18,9 +18,7 @@ struct GemmOut {
   int out_f64;          // 1: store double, 0: store float
   int accumulate;       // 1: C += alpha*result, 0: C = alpha*result
   float alpha;
-  const double* cin;
-  long long cin_ld;
-  double beta;
+  double diag;
   float* rhi;
   float* rlo;
   long long rld;
