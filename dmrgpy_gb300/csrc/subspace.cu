@@ -18,6 +18,8 @@
 // gets one more correction from a near-FP64 Gram matrix so that it is
 // orthonormal to ~1e-11 (a basis that is only FP32-orthonormal lets the norm
 // environment drift along the chain).
+#include <cuda_fp16.h>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -184,7 +186,8 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
     const int r = (int)(i / k), cc = (int)(i % k);
     const double a = A[i];
     B[i] = b * a + (r == cc ? c : 0.0);
-    mx = fmax(mx, fabs(a - (r == cc ? 1.0 : 0.0)));
+    const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
+    mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
   }
   // block max first, then one atomic per block (max of non-negative doubles
   // via their bit patterns): a per-thread atomic on one address serialises
@@ -200,26 +203,27 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
   }
 }
 
-__device__ __forceinline__ float tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+// FP16 operand pair of x * scale (scale a power of two that keeps |x scale|
+// inside the FP16 range): hi = fp16(x s), lo = fp16(x s - hi)
+__device__ __forceinline__ void split_h(double x, double scale, __half& hi, __half& lo) {
+  const double v = x * scale;
+  hi = __double2half(v);
+  lo = __double2half(v - static_cast<double>(__half2float(hi)));
 }
 
-// B = b*A + c*I (k x k) stored as the TF32 hi/lo operand pair [r][Kk] of the
-// next GEMM; also reports max|A - I| into *dev
-__global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, float* __restrict__ hi,
-                                  float* __restrict__ lo, int Kk, unsigned long long* __restrict__ dev) {
+// B = b*A + c*I (k x k) stored as the FP16 operand pair [r][Kk] (scaled) of
+// the next GEMM; also reports max|A - I| into *dev
+__global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, double scale,
+                                  __half* __restrict__ hi, __half* __restrict__ lo, int Kk,
+                                  unsigned long long* __restrict__ dev) {
   const long long total = (long long)k * k;
   double mx = 0.0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int r = (int)(i / k), cc = (int)(i % k);
     const double a = A[i];
-    const double v = b * a + (r == cc ? c : 0.0);
-    const float h = tf32_rn(static_cast<float>(v));
-    hi[(long long)r * Kk + cc] = h;
-    lo[(long long)r * Kk + cc] = tf32_rn(static_cast<float>(v - static_cast<double>(h)));
-    mx = fmax(mx, fabs(a - (r == cc ? 1.0 : 0.0)));
+    split_h(b * a + (r == cc ? c : 0.0), scale, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
+    const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
+    mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
   }
   __shared__ double red[32];
 #pragma unroll
@@ -233,9 +237,32 @@ __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b,
   }
 }
 
-inline int pad32s(long long x) { return (int)((x + 31) / 32 * 32); }
+// FP16 operand pairs of X (m x k, ld) in both layouts the iteration reads:
+// row-major xr[r][Kk] and transposed xt[c][Km] (through a 32 x 33 tile);
+// padding columns are written as zero
+__global__ void split_both_kernel(const double* __restrict__ X, long long ld, int m, int k, int Km, int Kk,
+                                  double scale, __half* __restrict__ xr_hi, __half* __restrict__ xr_lo,
+                                  __half* __restrict__ xt_hi, __half* __restrict__ xt_lo) {
+  __shared__ double t[32][33];
+  const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int j = ty; j < 32; j += 8) {
+    const int r = r0 + j, c = c0 + tx;
+    const double v = (r < m && c < k) ? X[(long long)r * ld + c] : 0.0;
+    t[j][tx] = v;
+    if (r < m && c < Kk) split_h(v, scale, xr_hi[(long long)r * Kk + c], xr_lo[(long long)r * Kk + c]);
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int c = c0 + j, r = r0 + tx;
+    if (c < k && r < Km) split_h(t[tx][j], scale, xt_hi[(long long)c * Km + r], xt_lo[(long long)c * Km + r]);
+  }
+}
 
-// TF32 hi/lo operand arrays of the polar iteration (fp32 [rows][K]):
+inline int pad64s(long long x) { return (int)((x + 63) / 64 * 64); }
+
+// FP16 operand arrays of the polar iteration ([rows][K] pairs of scaled
+// values, K padded to 64):
 //   xt  X^T [k][Km]  both operands of the Gram X^T X (K = m)
 //   xr  X   [m][Kk]  A operand of X B (K = k); two of them, because the
 //                    GEMM that reads one writes the next iterate's split
@@ -243,21 +270,24 @@ inline int pad32s(long long x) { return (int)((x + 31) / 32 * 32); }
 //   ps  c A + b I    B operand of the same product
 //   bs  B   [k][Kk]  B operand of X B (B is symmetric)
 // Each GEMM epilogue writes the splits the next GEMM reads, so the
-// iteration runs without separate split kernels.
+// iteration runs without separate split kernels.  The values are bounded
+// (|X| <= 1, |A| <= 1.5, |c A + b I| < 8, |B| < 14), so fixed power-of-two
+// scales keep every pair inside the FP16 range.
 struct PolarSplits {
-  float *xt_hi, *xt_lo, *xr_hi[2], *xr_lo[2], *as_hi, *as_lo, *ps_hi, *ps_lo, *bs_hi, *bs_lo;
+  __half *xt_hi, *xt_lo, *xr_hi[2], *xr_lo[2], *as_hi, *as_lo, *ps_hi, *ps_lo, *bs_hi, *bs_lo;
 };
+constexpr double SX = 4096.0, SA = 4096.0, SP = 4096.0, SB = 2048.0;
 
 size_t polar_split_bytes(int m, int k) {
-  const size_t Km = pad32s(m), Kk = pad32s(k), f = sizeof(float);
+  const size_t Km = pad64s(m), Kk = pad64s(k), f = sizeof(__half);
   return 2 * align_up(f * k * Km, 1024) + 4 * align_up(f * m * Kk, 1024) + 6 * align_up(f * k * Kk, 1024);
 }
 
 PolarSplits polar_splits(void* base, int m, int k) {
-  const size_t Km = pad32s(m), Kk = pad32s(k), f = sizeof(float);
+  const size_t Km = pad64s(m), Kk = pad64s(k), f = sizeof(__half);
   char* p = static_cast<char*>(base);
   auto take = [&](size_t n) {
-    float* r = reinterpret_cast<float*>(p);
+    __half* r = reinterpret_cast<__half*>(p);
     p += align_up(f * n, 1024);
     return r;
   };
@@ -314,21 +344,24 @@ int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, d
 int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
                unsigned long long* dev, void* gw, size_t gw_bytes, void* splits, int* err, bool exact,
                cudaStream_t s) {
-  const int Km = pad32s(m), Kk = pad32s(k);
+  const int Km = pad64s(m), Kk = pad64s(k);
   const PolarSplits ps = polar_splits(splits, m, k);
   // the K padding of the split arrays must read as zero
   if (Km != m || Kk != k) DMRG_CUDA_TRY(cudaMemsetAsync(splits, 0, polar_split_bytes(m, k), s));
-  // A = X^T X (FP64), optionally with its split for A A
+  const dim3 sgrid((k + 31) / 32, (Km > m ? Km : m) / 32 + 1);
+  if (sgrid.y > 65535) return DMRG_ERR_ARG;
+  // A = X^T X (FP64), optionally with its scaled split for A (c A + b I)
   auto gram = [&](bool with_split) -> int {
     GemmOut g{};
-    g.C = A; g.ldm = k; g.ldn = 1; g.M = k; g.N = k; g.out_f64 = 1; g.alpha = 1.f;
-    if (with_split) { g.rhi = ps.as_hi; g.rlo = ps.as_lo; g.rld = Kk; }
-    return tf32x3_gemm_split(ps.xt_hi, ps.xt_lo, ps.xt_hi, ps.xt_lo, k, k, Km, g, err, s);
+    g.C = A; g.ldm = k; g.ldn = 1; g.M = k; g.N = k; g.out_f64 = 1; g.alpha = (float)(1.0 / (SX * SX));
+    if (with_split) { g.rhi = ps.as_hi; g.rlo = ps.as_lo; g.rld = Kk; g.split_scale = SA; }
+    return f16x3_gemm_split(ps.xt_hi, ps.xt_lo, ps.xt_hi, ps.xt_lo, k, k, Km, g, err, s);
   };
   // an input that is already orthonormal (the usual warm start) skips the
   // iterations
   double d0 = 1.0;
-  DMRG_TRY(tf32x3_split_transpose(Z, ld, m, k, Km, ps.xt_hi, ps.xt_lo, s));
+  split_both_kernel<<<sgrid, 256, 0, s>>>(Z, ld, m, k, Km, Kk, SX, ps.xr_hi[0], ps.xr_lo[0], ps.xt_hi, ps.xt_lo);
+  DMRG_CHECK_LAUNCH();
   DMRG_TRY(gram(false));
   DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
   if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s) : DMRG_OK;
@@ -339,8 +372,8 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   DMRG_CHECK_LAUNCH();
   perturb_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, 1e-8 / sqrt((double)m), 0x5eed5ull + (unsigned)k);
   DMRG_CHECK_LAUNCH();
-  DMRG_TRY(tf32x3_split_transpose(Z, ld, m, k, Km, ps.xt_hi, ps.xt_lo, s));
-  DMRG_TRY(tf32x3_split_rows(Z, ld, m, k, Kk, ps.xr_hi[0], ps.xr_lo[0], s));
+  split_both_kernel<<<sgrid, 256, 0, s>>>(Z, ld, m, k, Km, Kk, SX, ps.xr_hi[0], ps.xr_lo[0], ps.xt_hi, ps.xt_lo);
+  DMRG_CHECK_LAUNCH();
   double* X = Z;
   double* Y = X2;
   int cur = 0;
@@ -353,24 +386,24 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
     DMRG_TRY(gram(q));
     // Y = X B, written with the next iterate's two splits
     GemmOut xb{};
-    xb.C = Y; xb.ldm = ld; xb.ldn = 1; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = 1.f;
+    xb.C = Y; xb.ldm = ld; xb.ldn = 1; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = (float)(1.0 / (SX * SB));
     xb.rhi = ps.xr_hi[1 - cur]; xb.rlo = ps.xr_lo[1 - cur]; xb.rld = Kk;
-    xb.thi = ps.xt_hi; xb.tlo = ps.xt_lo; xb.tld = Km;
+    xb.thi = ps.xt_hi; xb.tlo = ps.xt_lo; xb.tld = Km; xb.split_scale = SX;
     if (q) {
       // B = a I + A (b I + c A) (split only), so that X <- X B is the quintic
       // step a X + b X A + c X A^2 as one product
       const double a = 3.4445, b = -4.7750, c = 2.0315;
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, c, b, ps.ps_hi, ps.ps_lo, Kk, dev);
+      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       GemmOut b2{};
-      b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = 1.f; b2.diag = a;
-      b2.rhi = ps.bs_hi; b2.rlo = ps.bs_lo; b2.rld = Kk;
-      DMRG_TRY(tf32x3_gemm_split(ps.as_hi, ps.as_lo, ps.ps_hi, ps.ps_lo, k, k, Kk, b2, err, s));
+      b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)(1.0 / (SA * SP)); b2.diag = a;
+      b2.rhi = ps.bs_hi; b2.rlo = ps.bs_lo; b2.rld = Kk; b2.split_scale = SB;
+      DMRG_TRY(f16x3_gemm_split(ps.as_hi, ps.as_lo, ps.ps_hi, ps.ps_lo, k, k, Kk, b2, err, s));
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, ps.bs_hi, ps.bs_lo, Kk, dev);
+      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       unsigned long long h = 0;
       DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -378,7 +411,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
       memcpy(&d, &h, sizeof(d));
       if (d < 5e-6) break;
     }
-    DMRG_TRY(tf32x3_gemm_split(ps.xr_hi[cur], ps.xr_lo[cur], ps.bs_hi, ps.bs_lo, m, k, Kk, xb, err, s));
+    DMRG_TRY(f16x3_gemm_split(ps.xr_hi[cur], ps.xr_lo[cur], ps.bs_hi, ps.bs_lo, m, k, Kk, xb, err, s));
     double* t = X;
     X = Y;
     Y = t;
@@ -386,8 +419,8 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   }
   if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
   // a basis still far from orthonormal (a direction below the perturbation
-  // level) is reported instead of being corrected: the caller falls back to
-  // the FP64 SVD
+  // level, or a non-finite value) is reported instead of being corrected:
+  // the caller falls back to the FP64 SVD
   if (!(d < 1e-3)) return DMRG_ERR_NOCONV;
   if (exact) DMRG_TRY(orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s));
   return DMRG_OK;

@@ -17,6 +17,9 @@ constexpr long long WAIT_CYCLES = 4000000000ll;  // ~2 s at 2 GHz
 // one box row is one SWIZZLE_128B row of a K-major UMMA operand
 // (tf32x3.cu).
 int tma_map_k32(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows);
+// the same for a row-major fp16 array [rows][Kp] (Kp a multiple of 64): box
+// 64 x box_rows, one box row = one SWIZZLE_128B row
+int tma_map_k64h(CUtensorMap* m, const void* base, int rows, int Kp, int box_rows);
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -90,6 +93,22 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t ad, uint64_t b
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+// Instruction descriptor of kind::f16 with FP16 A and B (format 0), D fp32,
+// both K-major; one MMA covers K = 16 (32 bytes of a 128-byte swizzle row,
+// the same step as 8 tf32).
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+         (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
       "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 

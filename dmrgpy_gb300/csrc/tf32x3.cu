@@ -30,6 +30,8 @@
 #include <map>
 #include <mutex>
 
+#include <cuda_fp16.h>
+
 #include "tcgen05.cuh"
 #include "tf32x3.cuh"
 
@@ -56,6 +58,14 @@ __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
   lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
 }
 
+// FP16 pair of x * scale (scale a power of two chosen so that |x * scale|
+// stays below the FP16 maximum): hi = fp16(x s), lo = fp16(x s - hi)
+__device__ __forceinline__ void split2h(double x, double scale, __half& hi, __half& lo) {
+  const double v = x * scale;
+  hi = __double2half(v);
+  lo = __double2half(v - static_cast<double>(__half2float(hi)));
+}
+
 // Epilogue of the polar-iteration GEMMs (GemmOut with split outputs, a
 // diagonal term or no C): v = alpha*acc + diag*[row == col] (+ C if
 // accumulate), stored to C (FP64) if present and as TF32 hi/lo pairs,
@@ -63,12 +73,13 @@ __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
 // accumulates), so the stores of one tile overlap the next tile's MMAs; the
 // transposed pairs are written by consecutive lanes (= consecutive rows)
 // and so coalesce; the row-major ones use 16-byte stores where aligned.
-template <int BNT>
+template <int BNT, bool F16>
 __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out, int gm, int n0) {
   double* C = static_cast<double*>(out.C);
   const long long crow = (long long)gm * out.ldm;
   const bool full = n0 + BNT <= out.N;
   const bool cvec = full && C && out.ldn == 1 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) && out.ldm % 2 == 0;
+  // 4 split values per store: 16 bytes (tf32 pairs) or 8 bytes (fp16)
   const bool rvec = full && out.rhi && ((reinterpret_cast<uintptr_t>(out.rhi) & 15) == 0) &&
                     ((reinterpret_cast<uintptr_t>(out.rlo) & 15) == 0) && out.rld % 4 == 0;
 #pragma unroll
@@ -98,31 +109,67 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
       }
     }
     if (out.rhi || out.thi) {
-      float h[4], l[4];
+      if constexpr (F16) {
+        __half h[4], l[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) split2(v[j], h[j], l[j]);
-      if (out.rhi) {
-        float* ph = out.rhi + (long long)gm * out.rld + n0 + c;
-        float* pl = out.rlo + (long long)gm * out.rld + n0 + c;
-        if (rvec) {
-          *reinterpret_cast<float4*>(ph) = make_float4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<float4*>(pl) = make_float4(l[0], l[1], l[2], l[3]);
-        } else {
+        for (int j = 0; j < 4; ++j) split2h(v[j], out.split_scale, h[j], l[j]);
+        if (out.rhi) {
+          __half* ph = static_cast<__half*>(out.rhi) + (long long)gm * out.rld + n0 + c;
+          __half* pl = static_cast<__half*>(out.rlo) + (long long)gm * out.rld + n0 + c;
+          if (rvec) {
+            __half2 h01 = __halves2half2(h[0], h[1]), h23 = __halves2half2(h[2], h[3]);
+            __half2 l01 = __halves2half2(l[0], l[1]), l23 = __halves2half2(l[2], l[3]);
+            uint2 uh, ul;
+            uh.x = *reinterpret_cast<uint32_t*>(&h01); uh.y = *reinterpret_cast<uint32_t*>(&h23);
+            ul.x = *reinterpret_cast<uint32_t*>(&l01); ul.y = *reinterpret_cast<uint32_t*>(&l23);
+            *reinterpret_cast<uint2*>(ph) = uh;
+            *reinterpret_cast<uint2*>(pl) = ul;
+          } else {
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (n0 + c + j < out.N) {
-              ph[j] = h[j];
-              pl[j] = l[j];
-            }
+            for (int j = 0; j < 4; ++j)
+              if (n0 + c + j < out.N) {
+                ph[j] = h[j];
+                pl[j] = l[j];
+              }
+          }
         }
-      }
-      if (out.thi) {
+        if (out.thi) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int gn = n0 + c + j;
-          if (gn < out.N) {
-            out.thi[(long long)gn * out.tld + gm] = h[j];
-            out.tlo[(long long)gn * out.tld + gm] = l[j];
+          for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + c + j;
+            if (gn < out.N) {
+              static_cast<__half*>(out.thi)[(long long)gn * out.tld + gm] = h[j];
+              static_cast<__half*>(out.tlo)[(long long)gn * out.tld + gm] = l[j];
+            }
+          }
+        }
+      } else {
+        float h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) split2(v[j], h[j], l[j]);
+        if (out.rhi) {
+          float* ph = static_cast<float*>(out.rhi) + (long long)gm * out.rld + n0 + c;
+          float* pl = static_cast<float*>(out.rlo) + (long long)gm * out.rld + n0 + c;
+          if (rvec) {
+            *reinterpret_cast<float4*>(ph) = make_float4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<float4*>(pl) = make_float4(l[0], l[1], l[2], l[3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (n0 + c + j < out.N) {
+                ph[j] = h[j];
+                pl[j] = l[j];
+              }
+          }
+        }
+        if (out.thi) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + c + j;
+            if (gn < out.N) {
+              static_cast<float*>(out.thi)[(long long)gn * out.tld + gm] = h[j];
+              static_cast<float*>(out.tlo)[(long long)gn * out.tld + gm] = l[j];
+            }
           }
         }
       }
@@ -152,7 +199,7 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int
 // MMA warps run through the K-slices of consecutive tiles without a break
 // (the stage and TMEM rings continue across tiles), so loading and MMAs of
 // the next tile overlap the epilogue's stores of the current one.
-template <int BNT, bool EXTRA>
+template <int BNT, bool EXTRA, bool F16>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                        const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
@@ -160,6 +207,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   constexpr int TB_BYTES = BNT * BK * 4;                       // B tile
   constexpr int ST_BYTES = 2 * TILE_A_BYTES + 2 * TB_BYTES;    // one stage
   constexpr int STAGES = stages_of<BNT>();
+  // fp16 operands: one 128-byte swizzle row is 64 K-elements, split into two
+  // TMEM sub-slices of 32 so that the FP32 accumulation runs stay 32 long
+  constexpr int KE = F16 ? 64 : 32;      // K-elements per stage
+  constexpr int SUB = F16 ? 2 : 1;       // TMEM sub-slices per stage
+  constexpr int KK_SUB = (BK / 8) / SUB; // MMA K-steps per sub-slice
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
@@ -209,7 +261,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           }
           unsigned char* st = smem + s * ST_BYTES;
           mbar_expect_tx(&full[s], ST_BYTES);
-          const int x = kt * BK;
+          const int x = kt * KE;
           tma_load_2d(st, &mAhi, &full[s], x, m0);
           tma_load_2d(st + TILE_A_BYTES, &mAlo, &full[s], x, m0);
           tma_load_2d(st + 2 * TILE_A_BYTES, &mBhi, &full[s], x, n0);
@@ -219,36 +271,50 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      constexpr uint32_t idesc = idesc_tf32(BM, BNT);
-      long long g = 0;
+      constexpr uint32_t idesc = F16 ? idesc_f16(BM, BNT) : idesc_tf32(BM, BNT);
+      long long g = 0;    // stage counter
+      long long gs = 0;   // TMEM sub-slice counter
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        for (int kt = 0; kt < KT; ++kt, ++g) {
+        for (int kt = 0; kt < KT && ok; ++kt, ++g) {
           const int s = (int)(g % STAGES);
           const long long it = g / STAGES;
-          const int b = (int)(g % NACC);
-          const long long u = g / NACC;
-          if (!mbar_wait(&full[s], (uint32_t)(it & 1), err) ||
-              (g >= NACC && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), err))) {
+          if (!mbar_wait(&full[s], (uint32_t)(it & 1), err)) {
             ok = false;
             break;
           }
-          tc_fence_after();
-          const uint32_t d = tmem + b * BNT;
           const uint32_t base = smem_u32(smem + s * ST_BYTES);
           const uint32_t ahi = base, alo = base + TILE_A_BYTES;
           const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TB_BYTES;
 #pragma unroll
-          for (int kk = 0; kk < BK / 8; ++kk) {
-            const uint32_t o = kk * 32;  // 8 tf32 = 32 bytes along K inside the swizzle row
-            const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
-            const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
-            mma_tf32(d, dah, dbh, idesc, kk != 0);
-            mma_tf32(d, dah, dbl, idesc, 1u);
-            mma_tf32(d, dal, dbh, idesc, 1u);
+          for (int j = 0; j < SUB; ++j, ++gs) {
+            const int b = (int)(gs % NACC);
+            const long long u = gs / NACC;
+            if (gs >= NACC && !mbar_wait(&acc_empty[b], (uint32_t)((u - 1) & 1), err)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t d = tmem + b * BNT;
+#pragma unroll
+            for (int kq = 0; kq < KK_SUB; ++kq) {
+              // 32 bytes along K inside the swizzle row: 8 tf32 or 16 fp16
+              const uint32_t o = (j * KK_SUB + kq) * 32;
+              const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
+              const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
+              if constexpr (F16) {
+                mma_f16(d, dah, dbh, idesc, kq != 0);
+                mma_f16(d, dah, dbl, idesc, 1u);
+                mma_f16(d, dal, dbh, idesc, 1u);
+              } else {
+                mma_tf32(d, dah, dbh, idesc, kq != 0);
+                mma_tf32(d, dah, dbl, idesc, 1u);
+                mma_tf32(d, dal, dbh, idesc, 1u);
+              }
+            }
+            mma_commit(&acc_full[b]);
           }
-          mma_commit(&empty[s]);
-          mma_commit(&acc_full[b]);
+          if (ok) mma_commit(&empty[s]);
         }
       }
     }
@@ -264,7 +330,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       float acc[BNT];
 #pragma unroll
       for (int c = 0; c < BNT; ++c) acc[c] = 0.f;
-      for (int kt = 0; kt < KT && ok; ++kt, ++g) {
+      for (int kt = 0; kt < KT * SUB && ok; ++kt, ++g) {
         const int b = (int)(g % NACC);
         const long long u = g / NACC;
         ok = mbar_wait(&acc_full[b], (uint32_t)(u & 1), err);
@@ -285,7 +351,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       if (!ok) break;
       const int gm = m0 + row;
       if constexpr (EXTRA) {
-        if (gm < out.M) store_extra<BNT>(acc, out, gm, n0);
+        if (gm < out.M) store_extra<BNT, F16>(acc, out, gm, n0);
       } else {
       // full-width tiles of row-contiguous outputs are written with 16-byte
       // stores (4 floats / 2+2 doubles per step) instead of one element
@@ -560,15 +626,19 @@ int get_encoder() {
   return DMRG_OK;
 }
 
-// 2D fp32 row-major [rows][Kp] operand, box = (BK, box_rows), SWIZZLE_128B
-int make_map(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) {
-  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (Kp % BK) != 0) return DMRG_ERR_ARG;
+// 2D row-major [rows][Kp] operand, box = (one 128-byte row, box_rows),
+// SWIZZLE_128B: fp32 (32 per row, Kp % 32 == 0) or fp16 (64 per row,
+// Kp % 64 == 0)
+int make_map(CUtensorMap* m, const void* base, int rows, int Kp, int box_rows, bool f16 = false) {
+  const int ke = f16 ? 64 : BK, es = f16 ? 2 : 4;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (Kp % ke) != 0) return DMRG_ERR_ARG;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * es};
+  cuuint32_t box[2] = {(cuuint32_t)ke, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  CUresult r = g_encode(m, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                        const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? DMRG_OK : DMRG_ERR_ARG;
 }
@@ -580,9 +650,10 @@ int make_map(CUtensorMap* m, const float* base, int rows, int Kp, int box_rows) 
 // sweep are functions of (chi_l, chi_r, d, w), so a sweep tunes each of its
 // few shapes once.
 struct TuneKey {
-  int dev, M, N, K;
+  int dev, M, N, K, f16;
   bool operator<(const TuneKey& o) const {
     if (dev != o.dev) return dev < o.dev;
+    if (f16 != o.f16) return f16 < o.f16;
     if (M != o.M) return M < o.M;
     if (N != o.N) return N < o.N;
     return K < o.K;
@@ -597,10 +668,10 @@ std::mutex g_tune_mu;
 std::map<TuneKey, TuneVal> g_tune;
 std::atomic<int> g_tune_on{1};
 
-TuneKey tune_key(int M, int N, int K) {
+TuneKey tune_key(int M, int N, int K, bool f16) {
   int dev = 0;
   cudaGetDevice(&dev);
-  return TuneKey{dev, M, N, K};
+  return TuneKey{dev, M, N, K, f16 ? 1 : 0};
 }
 bool tune_enabled() { return g_tune_on.load() != 0; }
 struct GemmCfg;
@@ -641,18 +712,18 @@ int sm_count() {
   return n;
 }
 
-template <int BNT, bool EXTRA>
-int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const float* Bhi, const float* Blo, int M, int N,
+template <int BNT, bool EXTRA, bool F16>
+int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi, const void* Blo, int M, int N,
                   int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       gemm_smem_bytes(BNT)));
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA, F16>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem_bytes(BNT)));
     attr = true;
   }
   CUtensorMap mbh, mbl;
-  DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BNT));
-  DMRG_TRY(make_map(&mbl, Blo, N, Kp, BNT));
+  DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BNT, F16));
+  DMRG_TRY(make_map(&mbl, Blo, N, Kp, BNT, F16));
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BNT - 1) / BNT;
   const long long tiles = (long long)tiles_m * tiles_n;
   if (tiles > 0x7fffffffLL) return DMRG_ERR_ARG;
@@ -661,26 +732,33 @@ int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const float* B
   const int nsm = sm_count();
   if (nsm < 1) return DMRG_ERR_CUDA;
   const long long grid = tiles < nsm ? tiles : nsm;
-  tf32x3_gemm_kernel<BNT, EXTRA><<<(unsigned)grid, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
-      mah, mal, mbh, mbl, Kp / BK, tiles_m, tiles_n, g, out, err);
+  tf32x3_gemm_kernel<BNT, EXTRA, F16><<<(unsigned)grid, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
+      mah, mal, mbh, mbl, Kp / (F16 ? 64 : BK), tiles_m, tiles_n, g, out, err);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }
 
-int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
-               const GemmOut& out, int* err, cudaStream_t s) {
+template <bool F16>
+int gemm_launch_cfg(int bnt, bool extra, const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi,
+                    const void* Blo, int M, int N, int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
+  if (extra)
+    return bnt == 64 ? gemm_launch_t<64, true, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
+                     : gemm_launch_t<128, true, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
+  return bnt == 64 ? gemm_launch_t<64, false, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
+                   : gemm_launch_t<128, false, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
+}
+
+int gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, int M, int N, int Kp,
+               const GemmOut& out, int* err, cudaStream_t s, bool f16 = false) {
   DMRG_TRY(get_encoder());
   CUtensorMap mah, mal;
-  DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM));
-  DMRG_TRY(make_map(&mal, Alo, M, Kp, BM));
+  DMRG_TRY(make_map(&mah, Ahi, M, Kp, BM, f16));
+  DMRG_TRY(make_map(&mal, Alo, M, Kp, BM, f16));
   const bool extra = out.rhi || out.thi || !out.C || out.diag != 0.0;
   if (extra && !out.out_f64) return DMRG_ERR_ARG;
   auto launch = [&](const GemmCfg& c) -> int {
-    if (extra)
-      return c.bnt == 64 ? gemm_launch_t<64, true>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
-                         : gemm_launch_t<128, true>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
-    return c.bnt == 64 ? gemm_launch_t<64, false>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
-                       : gemm_launch_t<128, false>(mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
+    return f16 ? gemm_launch_cfg<true>(c.bnt, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
+               : gemm_launch_cfg<false>(c.bnt, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
   };
   const int tiles_m = (M + BM - 1) / BM;
   GemmCfg cfg{128, tiles_m};
@@ -689,7 +767,7 @@ int gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float
   // bit for bit: every output element sums the same K slices in the same
   // order whatever the tiling); accumulate-mode calls use the decision for
   // their shape if one exists, else 128-wide tiles in plain order.
-  const TuneKey key = tune_key(M, N, Kp);
+  const TuneKey key = tune_key(M, N, Kp, f16);
   if (!tune_lookup(key, &cfg)) {
     cfg = GemmCfg{128, tiles_m};
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -807,7 +885,17 @@ int launch_mpo_step_t(const Heff2Plan& p, cudaStream_t s) {
 
 int tf32x3_gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
                       const GemmOut& out, int* err, cudaStream_t s) {
-  return gemm_split(Ahi, Alo, Bhi, Blo, M, N, Kp, out, err, s);
+  return gemm_split(Ahi, Alo, Bhi, Blo, M, N, Kp, out, err, s, false);
+}
+
+int f16x3_gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, int M, int N, int Kp,
+                     const GemmOut& out, int* err, cudaStream_t s) {
+  return gemm_split(Ahi, Alo, Bhi, Blo, M, N, Kp, out, err, s, true);
+}
+
+int tma_map_k64h(CUtensorMap* m, const void* base, int rows, int Kp, int box_rows) {
+  DMRG_TRY(get_encoder());
+  return make_map(m, base, rows, Kp, box_rows, true);
 }
 
 int tf32x3_split_rows(const double* in, long long ld, int R, int K, int Kp, float* hi, float* lo, cudaStream_t s) {

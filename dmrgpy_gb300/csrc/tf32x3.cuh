@@ -19,18 +19,28 @@ struct GemmOut {
   int accumulate;       // 1: C += alpha*result, 0: C = alpha*result
   float alpha;
   double diag;
-  float* rhi;
-  float* rlo;
+  // split outputs: TF32 pairs (float) from the tf32 GEMM, FP16 pairs of
+  // v * split_scale (__half) from the fp16 GEMM
+  void* rhi;
+  void* rlo;
   long long rld;
-  float* thi;
-  float* tlo;
+  void* thi;
+  void* tlo;
   long long tld;
+  double split_scale;
 };
 
 // C (M x N) from split operands A (M x Kp) and B (N x Kp), fp32 [rows][Kp]
 // arrays holding TF32 hi/lo pairs (Kp a multiple of 32, zero beyond K)
 int tf32x3_gemm_split(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
                       const GemmOut& out, int* err, cudaStream_t s);
+// The same product from FP16 operand pairs ([rows][Kp] __half, Kp a
+// multiple of 64): two kind::f16 MMAs per K-step of 16 for the price of one
+// kind::tf32 step of 8, with the FP32 accumulation kept to 32-wide runs.
+// Operands are scaled by powers of two into the FP16 range; alpha carries
+// the inverse scales.
+int f16x3_gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, int M, int N, int Kp,
+                     const GemmOut& out, int* err, cudaStream_t s);
 // hi/lo[r][k] = split(in[r*ld + k]) (k < K, zero up to Kp)
 int tf32x3_split_rows(const double* in, long long ld, int R, int K, int Kp, float* hi, float* lo, cudaStream_t s);
 // hi/lo[c][r] = split(in[r*ld + c]) (r < R, zero up to Rp)
