@@ -212,6 +212,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   constexpr int KE = F16 ? 64 : 32;      // K-elements per stage
   constexpr int SUB = F16 ? 2 : 1;       // TMEM sub-slices per stage
   constexpr int KK_SUB = (BK / 8) / SUB; // MMA K-steps per sub-slice
+  // 64-wide tiles issue A_hi.[B_hi; B_lo] as one N = 128 MMA (two MMAs per
+  // K-step instead of three: the issuing thread's time per stage is as long
+  // as the MMAs' execution); their TMEM buffers are 128 columns wide
+  constexpr bool MERGE = BNT == 64;
+  constexpr int ACC_COLS = MERGE ? 2 * BNT : BNT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
@@ -237,7 +242,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(NACC * BNT));
+                 "r"(NACC * ACC_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   tc_fence_before();
@@ -272,6 +277,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = F16 ? idesc_f16(BM, BNT) : idesc_tf32(BM, BNT);
+      constexpr uint32_t idesc2 = F16 ? idesc_f16(BM, 2 * BNT) : idesc_tf32(BM, 2 * BNT);
       long long g = 0;    // stage counter
       long long gs = 0;   // TMEM sub-slice counter
       bool ok = true;
@@ -283,9 +289,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             ok = false;
             break;
           }
+          // descriptors of the stage's four tiles at K-step 0; a K-step of 32
+          // bytes adds 2 to the start-address field (address >> 4)
           const uint32_t base = smem_u32(smem + s * ST_BYTES);
-          const uint32_t ahi = base, alo = base + TILE_A_BYTES;
-          const uint32_t bhi = base + 2 * TILE_A_BYTES, blo = bhi + TB_BYTES;
+          const uint64_t dah0 = sdesc_sw128(base), dal0 = sdesc_sw128(base + TILE_A_BYTES);
+          const uint64_t dbh0 = sdesc_sw128(base + 2 * TILE_A_BYTES);
+          const uint64_t dbl0 = sdesc_sw128(base + 2 * TILE_A_BYTES + TB_BYTES);
 #pragma unroll
           for (int j = 0; j < SUB; ++j, ++gs) {
             const int b = (int)(gs % NACC);
@@ -295,21 +304,32 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
               break;
             }
             tc_fence_after();
-            const uint32_t d = tmem + b * BNT;
+            const uint32_t d = tmem + b * ACC_COLS;
 #pragma unroll
             for (int kq = 0; kq < KK_SUB; ++kq) {
               // 32 bytes along K inside the swizzle row: 8 tf32 or 16 fp16
-              const uint32_t o = (j * KK_SUB + kq) * 32;
-              const uint64_t dah = sdesc_sw128(ahi + o), dal = sdesc_sw128(alo + o);
-              const uint64_t dbh = sdesc_sw128(bhi + o), dbl = sdesc_sw128(blo + o);
-              if constexpr (F16) {
-                mma_f16(d, dah, dbh, idesc, kq != 0);
-                mma_f16(d, dah, dbl, idesc, 1u);
-                mma_f16(d, dal, dbh, idesc, 1u);
+              const uint64_t o = (uint64_t)((j * KK_SUB + kq) * 2);
+              if constexpr (MERGE) {
+                // A_hi . [B_hi; B_lo] (N = 2 BNT: the two B tiles are adjacent
+                // rows of one operand) into columns [0, 2 BNT), then A_lo . B_hi
+                // into columns [0, BNT); the epilogue adds the two halves
+                if constexpr (F16) {
+                  mma_f16(d, dah0 + o, dbh0 + o, idesc2, kq != 0);
+                  mma_f16(d, dal0 + o, dbh0 + o, idesc, 1u);
+                } else {
+                  mma_tf32(d, dah0 + o, dbh0 + o, idesc2, kq != 0);
+                  mma_tf32(d, dal0 + o, dbh0 + o, idesc, 1u);
+                }
               } else {
-                mma_tf32(d, dah, dbh, idesc, kq != 0);
-                mma_tf32(d, dah, dbl, idesc, 1u);
-                mma_tf32(d, dal, dbh, idesc, 1u);
+                if constexpr (F16) {
+                  mma_f16(d, dah0 + o, dbh0 + o, idesc, kq != 0);
+                  mma_f16(d, dah0 + o, dbl0 + o, idesc, 1u);
+                  mma_f16(d, dal0 + o, dbh0 + o, idesc, 1u);
+                } else {
+                  mma_tf32(d, dah0 + o, dbh0 + o, idesc, kq != 0);
+                  mma_tf32(d, dah0 + o, dbl0 + o, idesc, 1u);
+                  mma_tf32(d, dal0 + o, dbh0 + o, idesc, 1u);
+                }
               }
             }
             mma_commit(&acc_full[b]);
@@ -337,11 +357,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         tc_fence_after();
         if (ok) {
 #pragma unroll
-          for (int c = 0; c < BNT; c += 64) {
+          for (int c = 0; c < ACC_COLS; c += 64) {
             float v[64];
-            tmem_ld64(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * BNT + c, v);
+            tmem_ld64(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * ACC_COLS + c, v);
 #pragma unroll
-            for (int j = 0; j < 64; ++j) acc[c + j] += v[j];
+            for (int j = 0; j < 64; ++j) acc[(c + j) % BNT] += v[j];
           }
         }
         tc_fence_before();
@@ -424,7 +444,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * BNT));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NACC * ACC_COLS));
   }
 }
 
