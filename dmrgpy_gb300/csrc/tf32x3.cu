@@ -45,7 +45,6 @@ constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
 // 64-wide (a stage's TMA round trip is ~2 us under load, so the bytes in
 // flight bound the K-slice rate)
 template <int BNT> __host__ __device__ constexpr int stages_of() { return BNT == 64 ? 4 : 3; }
-constexpr int NACC = 4;     // TMEM accumulator buffers (one K-slice each)
 constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 // dynamic shared memory of the GEMM for an N-tile width of bnt columns
 constexpr int gemm_smem_bytes(int bnt) {
@@ -199,7 +198,7 @@ __device__ __forceinline__ void tile_origin(int t, int tiles_m, int tiles_n, int
 // MMA warps run through the K-slices of consecutive tiles without a break
 // (the stage and TMEM rings continue across tiles), so loading and MMAs of
 // the next tile overlap the epilogue's stores of the current one.
-template <int BNT, bool EXTRA, bool F16>
+template <int BNT, bool EXTRA, bool F16, bool MERGE>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tf32x3_gemm_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
                        const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int KT,
@@ -212,11 +211,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   constexpr int KE = F16 ? 64 : 32;      // K-elements per stage
   constexpr int SUB = F16 ? 2 : 1;       // TMEM sub-slices per stage
   constexpr int KK_SUB = (BK / 8) / SUB; // MMA K-steps per sub-slice
-  // 64-wide tiles issue A_hi.[B_hi; B_lo] as one N = 128 MMA (two MMAs per
-  // K-step instead of three: the issuing thread's time per stage is as long
-  // as the MMAs' execution); their TMEM buffers are 128 columns wide
-  constexpr bool MERGE = BNT == 64;
+  // MERGE issues A_hi.[B_hi; B_lo] as one N = 2 BNT MMA (two MMAs per
+  // K-step instead of three: a single thread issues ~25 ns per MMA, about
+  // as long as 12 MMAs of a stage take to execute); its TMEM buffers are
+  // 2 BNT columns wide, so a 128-wide tile keeps two of them, not four
   constexpr int ACC_COLS = MERGE ? 2 * BNT : BNT;
+  constexpr int NACC = (512 / ACC_COLS) < 4 ? (512 / ACC_COLS) : 4;   // TMEM ring of K-slice buffers
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
@@ -681,6 +681,7 @@ struct TuneKey {
 };
 struct TuneVal {
   int bnt;
+  int merge;
   int group;
   float ms;
 };
@@ -698,10 +699,11 @@ struct GemmCfg;
 bool tune_lookup(const TuneKey& k, GemmCfg* cfg);
 void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms);
 
-// Launch configuration of one split GEMM: N-tile width (128 or 64 columns)
-// and grouped tile order.
+// Launch configuration of one split GEMM: N-tile width (128 or 64 columns),
+// whether the two B splits go into one MMA, and grouped tile order.
 struct GemmCfg {
   int bnt;
+  int merge;
   int group;
 };
 
@@ -709,12 +711,12 @@ bool tune_lookup(const TuneKey& k, GemmCfg* cfg) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
   auto it = g_tune.find(k);
   if (it == g_tune.end()) return false;
-  *cfg = GemmCfg{it->second.bnt, it->second.group};
+  *cfg = GemmCfg{it->second.bnt, it->second.merge, it->second.group};
   return true;
 }
 void tune_store(const TuneKey& k, const GemmCfg& cfg, float ms) {
   std::lock_guard<std::mutex> lock(g_tune_mu);
-  g_tune[k] = TuneVal{cfg.bnt, cfg.group, ms};
+  g_tune[k] = TuneVal{cfg.bnt, cfg.merge, cfg.group, ms};
 }
 
 // multiprocessor count of the current device (cached per device)
@@ -732,12 +734,12 @@ int sm_count() {
   return n;
 }
 
-template <int BNT, bool EXTRA, bool F16>
+template <int BNT, bool EXTRA, bool F16, bool MERGE>
 int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi, const void* Blo, int M, int N,
                   int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA, F16>,
+    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA, F16, MERGE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem_bytes(BNT)));
     attr = true;
   }
@@ -752,20 +754,24 @@ int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const void* Bh
   const int nsm = sm_count();
   if (nsm < 1) return DMRG_ERR_CUDA;
   const long long grid = tiles < nsm ? tiles : nsm;
-  tf32x3_gemm_kernel<BNT, EXTRA, F16><<<(unsigned)grid, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
+  tf32x3_gemm_kernel<BNT, EXTRA, F16, MERGE><<<(unsigned)grid, GEMM_THREADS, gemm_smem_bytes(BNT), s>>>(
       mah, mal, mbh, mbl, Kp / (F16 ? 64 : BK), tiles_m, tiles_n, g, out, err);
   DMRG_CHECK_LAUNCH();
   return DMRG_OK;
 }
 
 template <bool F16>
-int gemm_launch_cfg(int bnt, bool extra, const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi,
+int gemm_launch_cfg(int bnt, int merge, bool extra, const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi,
                     const void* Blo, int M, int N, int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
-  if (extra)
-    return bnt == 64 ? gemm_launch_t<64, true, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
-                     : gemm_launch_t<128, true, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
-  return bnt == 64 ? gemm_launch_t<64, false, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
-                   : gemm_launch_t<128, false, F16>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
+  // 64-wide tiles always merge; 128-wide tiles either way (tuned)
+  if (bnt == 64)
+    return extra ? gemm_launch_t<64, true, F16, true>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
+                 : gemm_launch_t<64, false, F16, true>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
+  if (merge)
+    return extra ? gemm_launch_t<128, true, F16, true>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
+                 : gemm_launch_t<128, false, F16, true>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
+  return extra ? gemm_launch_t<128, true, F16, false>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s)
+               : gemm_launch_t<128, false, F16, false>(mah, mal, Bhi, Blo, M, N, Kp, group, out, err, s);
 }
 
 int gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Blo, int M, int N, int Kp,
@@ -777,11 +783,11 @@ int gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Bl
   const bool extra = out.rhi || out.thi || !out.C || out.diag != 0.0;
   if (extra && !out.out_f64) return DMRG_ERR_ARG;
   auto launch = [&](const GemmCfg& c) -> int {
-    return f16 ? gemm_launch_cfg<true>(c.bnt, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
-               : gemm_launch_cfg<false>(c.bnt, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
+    return f16 ? gemm_launch_cfg<true>(c.bnt, c.merge, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
+               : gemm_launch_cfg<false>(c.bnt, c.merge, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
   };
   const int tiles_m = (M + BM - 1) / BM;
-  GemmCfg cfg{128, tiles_m};
+  GemmCfg cfg{128, 0, tiles_m};
   // Tile width and order are tuned per GEMM shape on its first
   // overwrite-mode call (re-running an overwrite GEMM reproduces its output
   // bit for bit: every output element sums the same K slices in the same
@@ -789,18 +795,19 @@ int gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Bl
   // their shape if one exists, else 128-wide tiles in plain order.
   const TuneKey key = tune_key(M, N, Kp, f16);
   if (!tune_lookup(key, &cfg)) {
-    cfg = GemmCfg{128, tiles_m};
+    cfg = GemmCfg{128, 0, tiles_m};
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     DMRG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
     const long long tiles128 = (long long)tiles_m * ((N + 127) / 128);
     if (tune_enabled() && !out.accumulate && cap == cudaStreamCaptureStatusNone && tiles128 >= 48) {
-      const GemmCfg cand[6] = {{128, tiles_m}, {128, 16}, {128, 8}, {64, tiles_m}, {64, 16}, {64, 8}};
+      const GemmCfg cand[9] = {{128, 0, tiles_m}, {128, 0, 16}, {128, 0, 8}, {128, 1, tiles_m}, {128, 1, 16},
+                               {128, 1, 8},       {64, 1, tiles_m}, {64, 1, 16}, {64, 1, 8}};
       float best = 0.f;
       bool have = false;
       cudaEvent_t e0, e1;
       DMRG_CUDA_TRY(cudaEventCreate(&e0));
       DMRG_CUDA_TRY(cudaEventCreate(&e1));
-      for (int i = 0; i < 6; ++i) {
+      for (int i = 0; i < 9; ++i) {
         GemmCfg c = cand[i];
         if (c.group > tiles_m) c.group = tiles_m;
         if (i % 3 != 0 && c.group == tiles_m) continue;   // same as the plain order
@@ -1288,13 +1295,14 @@ extern "C" int dmrg_autotune_entries(int* out, int max_entries) {
   int n = 0;
   for (const auto& kv : dmrg::g_tune) {
     if (out && n < max_entries) {
-      int* e = out + 6 * n;
+      int* e = out + 7 * n;
       e[0] = kv.first.M;
       e[1] = kv.first.N;
       e[2] = kv.first.K;
       e[3] = kv.second.bnt;
-      e[4] = kv.second.group;
-      e[5] = (int)(kv.second.ms * 1000.f);
+      e[4] = kv.second.merge;
+      e[5] = kv.second.group;
+      e[6] = (int)(kv.second.ms * 1000.f);
     }
     ++n;
   }

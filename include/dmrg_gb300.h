@@ -236,9 +236,9 @@ int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* s
  * call in Python, pyitensor/kernels.py:298-334). */
 /* Turn tuning of new shapes on (1, the default) or off; returns the previous setting. */
 int dmrg_autotune_enable(int enable);
-/* Copies up to max_entries decisions as 6 ints each (M, N, K, tile width,
- * group, best time in microseconds) into out (may be NULL); returns the
- * number held. */
+/* Copies up to max_entries decisions as 7 ints each (M, N, K, tile width,
+ * 1 if the two B splits are issued as one MMA, group, best time in
+ * microseconds) into out (may be NULL); returns the number held. */
 int dmrg_autotune_entries(int* out, int max_entries);
 
 /* ---- many independent chains at once (FP64 / complex FP64) ----------------

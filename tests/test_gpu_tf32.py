@@ -109,10 +109,10 @@ def test_gemm_tile_order_tuner_changes_nothing_but_speed():
     scale = np.max(np.abs(C0))
     assert np.max(np.abs(C0 - C1)) <= 1e-6 * scale and np.array_equal(C1, C2)
     count = lib.dmrg_autotune_entries(None, 0)
-    buf = (ctypes.c_int * (6 * max(count, 1)))()
+    buf = (ctypes.c_int * (7 * max(count, 1)))()
     lib.dmrg_autotune_entries(buf, count)
-    shapes = [tuple(buf[6 * i:6 * i + 5]) for i in range(count)]
-    assert all(s[3] in (64, 128) for s in shapes), shapes
+    shapes = [tuple(buf[7 * i:7 * i + 6]) for i in range(count)]
+    assert all(s[3] in (64, 128) and s[4] in (0, 1) for s in shapes), shapes
     assert any(s[0] == m and s[1] == n for s in shapes), shapes
     assert np.max(np.abs(C1 - A @ B)) / np.max(np.abs(A @ B)) < TOL
 
