@@ -135,14 +135,22 @@ int transpose(const double* src, long long lds, int rows, int cols, double* dst,
 // a tiny random perturbation) become orthonormal completions, so the result
 // is orthonormal whatever the conditioning of Z.
 
-__global__ void scale_cols_kernel(double* __restrict__ Z, long long ld, int m, int k, const double* __restrict__ n2,
-                                  double extra) {
-  const long long total = (long long)m * k;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / k), c = (int)(i % k);
-    const double nn = n2[c];
-    Z[(long long)r * ld + c] = nn > 0.0 ? Z[(long long)r * ld + c] * (extra / sqrt(nn)) : 0.0;
-  }
+// f[c] = extra / |Z[:, c]| (0 for a zero column), from the squared norms
+__global__ void col_factor_kernel(double* __restrict__ n2, int k, double extra) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < k) n2[c] = n2[c] > 0.0 ? extra / sqrt(n2[c]) : 0.0;
+}
+
+// Z[r][c] = Z[r][c] f[c] + eps u(r k + c), u uniform in [-1/2, 1/2): unit
+// columns scaled by 1/sqrt(k), plus a tiny random perturbation that keeps
+// exactly dependent directions from staying at 0.  Row r = blockIdx.y.
+__global__ void scale_perturb_kernel(double* __restrict__ Z, long long ld, int k, const double* __restrict__ f,
+                                     double eps, unsigned long long seed) {
+  const int r = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  const long long i = (long long)r * k + c;
+  double* z = Z + (long long)r * ld + c;
+  *z = *z * f[c] + eps * static_cast<double>(hash_uniform(seed, i));
 }
 
 // n2[c] = sum_r Z[r][c]^2: one block per 32 columns, 32 row lanes per
@@ -168,26 +176,18 @@ __global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ 
   }
 }
 
-// Z += eps * (random), keeps exactly dependent directions from staying at 0
-__global__ void perturb_kernel(double* __restrict__ Z, long long ld, int m, int k, double eps, unsigned long long seed) {
-  const long long total = (long long)m * k;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / k), c = (int)(i % k);
-    Z[(long long)r * ld + c] += eps * static_cast<double>(hash_uniform(seed, i));
-  }
-}
-
-// B = b*A + c*I  (k x k), also reports max|A - I| into *dev
+// B = b*A + c*I  (k x k), also reports max|A - I| into *dev (row r =
+// blockIdx.y, columns over blockIdx.x)
 __global__ void poly_kernel(const double* __restrict__ A, int k, double b, double c, double* __restrict__ B,
                             unsigned long long* __restrict__ dev) {
-  const long long total = (long long)k * k;
+  const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
   double mx = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / k), cc = (int)(i % k);
+  if (cc < k) {
+    const long long i = (long long)r * k + cc;
     const double a = A[i];
     B[i] = b * a + (r == cc ? c : 0.0);
     const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
-    mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
+    mx = dv == dv ? dv : INFINITY;   // a non-finite entry reports +inf
   }
   // block max first, then one atomic per block (max of non-negative doubles
   // via their bit patterns): a per-thread atomic on one address serialises
@@ -216,14 +216,14 @@ __device__ __forceinline__ void split_h(double x, double scale, __half& hi, __ha
 __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, double scale,
                                   __half* __restrict__ hi, __half* __restrict__ lo, int Kk,
                                   unsigned long long* __restrict__ dev) {
-  const long long total = (long long)k * k;
+  // row r = blockIdx.y, columns over blockIdx.x
+  const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
   double mx = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / k), cc = (int)(i % k);
-    const double a = A[i];
+  if (cc < k) {
+    const double a = A[(long long)r * k + cc];
     split_h(b * a + (r == cc ? c : 0.0), scale, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
     const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
-    mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
+    mx = dv == dv ? dv : INFINITY;   // a non-finite entry reports +inf
   }
   __shared__ double red[32];
 #pragma unroll
@@ -324,7 +324,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
   if (st == DMRG_ERR_ARG || st == DMRG_ERR_WORKSPACE) DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
   else DMRG_TRY(st);
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
+  poly_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
   DMRG_CHECK_LAUNCH();
   return tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s);
 }
@@ -332,7 +332,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
 // max|A - I| of a k x k Gram matrix (host value; synchronises the stream)
 int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, double* out, cudaStream_t s) {
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
+  poly_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
   DMRG_CHECK_LAUNCH();
   unsigned long long h = 0;
   DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -349,7 +349,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   // the K padding of the split arrays must read as zero
   if (Km != m || Kk != k) DMRG_CUDA_TRY(cudaMemsetAsync(splits, 0, polar_split_bytes(m, k), s));
   const dim3 sgrid((k + 31) / 32, (Km > m ? Km : m) / 32 + 1);
-  if (sgrid.y > 65535) return DMRG_ERR_ARG;
+  if (sgrid.y > 65535 || m > 65535 || k > 65535) return DMRG_ERR_ARG;
   // A = X^T X (FP64), optionally with its scaled split for A (c A + b I)
   auto gram = [&](bool with_split) -> int {
     GemmOut g{};
@@ -368,9 +368,10 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
   colsq_kernel<<<(k + 31) / 32, 1024, 0, s>>>(Z, ld, m, k, n2);
   DMRG_CHECK_LAUNCH();
-  scale_cols_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, n2, 1.0 / sqrt((double)k));
+  col_factor_kernel<<<(k + 255) / 256, 256, 0, s>>>(n2, k, 1.0 / sqrt((double)k));
   DMRG_CHECK_LAUNCH();
-  perturb_kernel<<<egrid((long long)m * k), 256, 0, s>>>(Z, ld, m, k, 1e-8 / sqrt((double)m), 0x5eed5ull + (unsigned)k);
+  scale_perturb_kernel<<<dim3((k + 255) / 256, m), 256, 0, s>>>(Z, ld, k, n2, 1e-8 / sqrt((double)m),
+                                                                0x5eed5ull + (unsigned)k);
   DMRG_CHECK_LAUNCH();
   split_both_kernel<<<sgrid, 256, 0, s>>>(Z, ld, m, k, Km, Kk, SX, ps.xr_hi[0], ps.xr_lo[0], ps.xt_hi, ps.xt_lo);
   DMRG_CHECK_LAUNCH();
@@ -394,7 +395,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
       // step a X + b X A + c X A^2 as one product
       const double a = 3.4445, b = -4.7750, c = 2.0315;
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
+      poly_split_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       GemmOut b2{};
       b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)(1.0 / (SA * SP)); b2.diag = a;
@@ -403,7 +404,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<egrid((long long)k * k), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
+      poly_split_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       unsigned long long h = 0;
       DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
