@@ -176,19 +176,21 @@ __global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ 
   }
 }
 
-// B = b*A + c*I  (k x k), also reports max|A - I| into *dev (row r =
-// blockIdx.y, columns over blockIdx.x)
+// B = b*A + c*I  (k x k), also reports max|A - I| into *dev.  A block
+// covers POLY_ROWS whole rows, so the grid ends in k / POLY_ROWS atomics on
+// *dev (one per block), not one per 256 elements.
+constexpr int POLY_ROWS = 8;
 __global__ void poly_kernel(const double* __restrict__ A, int k, double b, double c, double* __restrict__ B,
                             unsigned long long* __restrict__ dev) {
-  const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
   double mx = 0.0;
-  if (cc < k) {
-    const long long i = (long long)r * k + cc;
-    const double a = A[i];
-    B[i] = b * a + (r == cc ? c : 0.0);
-    const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
-    mx = dv == dv ? dv : INFINITY;   // a non-finite entry reports +inf
-  }
+  for (int r = blockIdx.y * POLY_ROWS; r < k && r < (blockIdx.y + 1) * POLY_ROWS; ++r)
+    for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
+      const long long i = (long long)r * k + cc;
+      const double a = A[i];
+      B[i] = b * a + (r == cc ? c : 0.0);
+      const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
+      mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
+    }
   // block max first, then one atomic per block (max of non-negative doubles
   // via their bit patterns): a per-thread atomic on one address serialises
   __shared__ double red[32];
@@ -216,15 +218,15 @@ __device__ __forceinline__ void split_h(double x, double scale, __half& hi, __ha
 __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, double scale,
                                   __half* __restrict__ hi, __half* __restrict__ lo, int Kk,
                                   unsigned long long* __restrict__ dev) {
-  // row r = blockIdx.y, columns over blockIdx.x
-  const int r = blockIdx.y, cc = blockIdx.x * blockDim.x + threadIdx.x;
+  // POLY_ROWS whole rows per block (one atomic per block)
   double mx = 0.0;
-  if (cc < k) {
-    const double a = A[(long long)r * k + cc];
-    split_h(b * a + (r == cc ? c : 0.0), scale, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
-    const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
-    mx = dv == dv ? dv : INFINITY;   // a non-finite entry reports +inf
-  }
+  for (int r = blockIdx.y * POLY_ROWS; r < k && r < (blockIdx.y + 1) * POLY_ROWS; ++r)
+    for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
+      const double a = A[(long long)r * k + cc];
+      split_h(b * a + (r == cc ? c : 0.0), scale, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
+      const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
+      mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
+    }
   __shared__ double red[32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -324,7 +326,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
   if (st == DMRG_ERR_ARG || st == DMRG_ERR_WORKSPACE) DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
   else DMRG_TRY(st);
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
+  poly_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
   DMRG_CHECK_LAUNCH();
   return tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s);
 }
@@ -332,7 +334,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
 // max|A - I| of a k x k Gram matrix (host value; synchronises the stream)
 int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, double* out, cudaStream_t s) {
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
+  poly_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
   DMRG_CHECK_LAUNCH();
   unsigned long long h = 0;
   DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -395,7 +397,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
       // step a X + b X A + c X A^2 as one product
       const double a = 3.4445, b = -4.7750, c = 2.0315;
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
+      poly_split_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       GemmOut b2{};
       b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)(1.0 / (SA * SP)); b2.diag = a;
@@ -404,7 +406,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<dim3((k + 255) / 256, k), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
+      poly_split_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       unsigned long long h = 0;
       DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
