@@ -204,9 +204,13 @@ int dmrg_svd_truncate(int dtype, int m, int n, const void* M,
 
 /* Fixed-rank truncation for the split-TF32 sweep when maxdim binds
  * (cutoff <= 0): keeps k = maxdim vectors found by warm-started subspace
- * iteration with polar (Newton-Schulz) orthonormalisation (all contractions
- * split-TF32 on tcgen05) and an FP64-Gram correction of the kept basis,
- * instead of a full SVD.  Real dtype.
+ * iteration (products with theta split-TF32 on tcgen05), polar
+ * (Newton-Schulz) orthonormalisation on FP16-split tcgen05 GEMMs, and one
+ * correction of the kept basis from a near-FP64 Gram matrix (dmrg_gram's
+ * digit method), instead of a full SVD.  Real dtype.  A basis the polar
+ * iteration cannot orthonormalise (a direction below its 1e-8 floor, or a
+ * non-finite value) returns DMRG_ERR_NOCONV: the caller falls back to
+ * dmrg_svd_truncate.
  *   absorb 0: left_out (m x k) orthonormal columns, right_out = left^T theta
  *             (k x n); start = the current RIGHT tensor as kstart x n
  *             (orthonormal rows in a right-canonical MPS)
