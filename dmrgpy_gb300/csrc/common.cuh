@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cuComplex.h>
+#include <atomic>
 #include <cstdint>
 #include <cstddef>
 
@@ -85,6 +86,19 @@ void uncount_launches(unsigned long long n);  // launches made during a graph ca
     int _s = (x);                                                \
     if (_s != DMRG_OK) return _s;                                \
   } while (0)
+
+// Raises a kernel's dynamic shared-memory limit once per device: the
+// attribute belongs to the device, and a process may drive several.  `done`
+// (one per kernel and size) records the devices already set.
+inline int smem_attr_once(const void* fn, int bytes, std::atomic<unsigned long long>& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DMRG_ERR_CUDA;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return DMRG_OK;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return DMRG_ERR_CUDA;
+  done.fetch_or(bit, std::memory_order_release);
+  return DMRG_OK;
+}
 
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 

@@ -373,11 +373,8 @@ int gram_digits(const double* X, long long ld, int m, int k, double* G, void* wo
     DMRG_TRY(tma_map_k32(&ma[i], ops[i], k, Kp, GM));
     DMRG_TRY(tma_map_k32(&mb[i], ops[i], k, Kp, GN));
   }
-  static bool attr = false;
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(gram_digits_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GRAM_SMEM));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(gram_digits_kernel), GRAM_SMEM, attr));
   const int tiles_m = (k + GM - 1) / GM, tiles_n = (k + GN - 1) / GN;
   long long tiles = 0;
   for (int mi = 0; mi < tiles_m; ++mi) tiles += tiles_n - TPR * mi > 0 ? tiles_n - TPR * mi : 0;

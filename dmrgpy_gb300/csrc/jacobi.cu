@@ -529,12 +529,9 @@ int hestenes_factor(const T* M, int m, int n, int left, void* work, double* host
     if (xbytes <= 160 * 1024) {
       a.X_in_smem = 1;
       smem = xbytes;
-      static bool attr = false;
-      if (!attr) {
-        DMRG_CUDA_TRY(cudaFuncSetAttribute(hestenes_kernel<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-        DMRG_CUDA_TRY(cudaFuncSetAttribute(hestenes_kernel<cplx, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
-        attr = true;
-      }
+      static std::atomic<unsigned long long> attr_d{0}, attr_z{0};
+      DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(hestenes_kernel<double, false>), 160 * 1024, attr_d));
+      DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(hestenes_kernel<cplx, false>), 160 * 1024, attr_z));
     }
     hestenes_kernel<T, false><<<1, threads, smem, s>>>(a);
     DMRG_CHECK_LAUNCH();

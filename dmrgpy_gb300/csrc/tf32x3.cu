@@ -737,12 +737,9 @@ int sm_count() {
 template <int BNT, bool EXTRA, bool F16, bool MERGE>
 int gemm_launch_t(const CUtensorMap& mah, const CUtensorMap& mal, const void* Bhi, const void* Blo, int M, int N,
                   int Kp, int group, const GemmOut& out, int* err, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(tf32x3_gemm_kernel<BNT, EXTRA, F16, MERGE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, gemm_smem_bytes(BNT)));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(tf32x3_gemm_kernel<BNT, EXTRA, F16, MERGE>),
+                          gemm_smem_bytes(BNT), attr));
   CUtensorMap mbh, mbl;
   DMRG_TRY(make_map(&mbh, Bhi, N, Kp, BNT, F16));
   DMRG_TRY(make_map(&mbl, Blo, N, Kp, BNT, F16));
@@ -893,12 +890,8 @@ int launch_mpo_step_t(const Heff2Plan& p, cudaStream_t s) {
   const int cpad = (nst * p.wl + 3) & ~3;
   const size_t smem = sizeof(float) * (size_t)nst * p.wr * cpad + sizeof(int) * MAXC;
   if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
-  static bool attr = false;
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_t_kernel<MAXC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       200 * 1024));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(mpo_step_t_kernel<MAXC>), 200 * 1024, attr));
   dim3 grid((p.cr + 31) / 32, (p.cl + RT_A - 1) / RT_A);
   if (grid.y > 65535) return DMRG_ERR_ARG;
   mpo_step_t_kernel<MAXC><<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi,
@@ -993,11 +986,8 @@ int mpo_step_generic(const Heff2Plan& p, cudaStream_t s) {
   const int nst = p.d1 * p.d2;
   const size_t smem = sizeof(float) * ((size_t)nst * p.wr * nst * p.wl + (size_t)MID_AT * nst * p.wl * 32);
   if (smem > 200 * 1024) return DMRG_ERR_UNSUPPORTED;
-  static bool attr = false;
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(mpo_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr{0};
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(mpo_step_kernel), 200 * 1024, attr));
   dim3 grid((p.cr + 31) / 32, (p.cl + MID_AT - 1) / MID_AT);
   if (grid.y > 65535) return DMRG_ERR_ARG;
   mpo_step_kernel<<<grid, 256, smem, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, p.X3_hi, p.X3_lo);
@@ -1235,12 +1225,9 @@ int tf32x3_env(int side, int cl, int d, int cr, int wl, int wr, const double* E,
                double* Enew, void* work, cudaStream_t s) {
   EnvPlan p = env_plan(side, cl, d, cr, wl, wr, work);
   DMRG_CUDA_TRY(cudaMemsetAsync(p.err, 0, 256, s));
-  static bool attr = false;
-  if (!attr) {
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(env_left_mpo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    DMRG_CUDA_TRY(cudaFuncSetAttribute(env_right_mpo_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr = true;
-  }
+  static std::atomic<unsigned long long> attr_l{0}, attr_r{0};
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(env_left_mpo_kernel), 200 * 1024, attr_l));
+  DMRG_TRY(smem_attr_once(reinterpret_cast<const void*>(env_right_mpo_kernel), 200 * 1024, attr_r));
   if (side == 0) {
     // GEMM 1: rows (s,b) of A^T, cols (a',k) of L, K = a
     DMRG_TRY(split_transpose(A, (long long)d * cr, cl, d * cr, p.Kp1, p.A1hi, p.A1lo, s));
