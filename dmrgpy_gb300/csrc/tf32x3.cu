@@ -47,11 +47,8 @@ constexpr int BK = 32;      // fp32 per K-slice = 128 bytes = one SW128 row
 template <int BNT> __host__ __device__ constexpr int stages_of() { return BNT == 64 ? 4 : 3; }
 constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 // dynamic shared memory of the GEMM for an N-tile width of bnt columns
-// epilogue staging: a 32 x 33 fp32 tile per epilogue warp
-constexpr int STG_LD = 33;
-constexpr int STG_BYTES = 4 * 32 * STG_LD * 4;
 constexpr int gemm_smem_bytes(int bnt) {
-  return (bnt == 64 ? 4 : 3) * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + STG_BYTES + 1024 + 256;
+  return (bnt == 64 ? 4 : 3) * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256;
 }
 constexpr int GEMM_THREADS = 192;           // 6 warps
 
@@ -68,86 +65,114 @@ __device__ __forceinline__ void split2h(double x, double scale, __half& hi, __ha
   lo = __double2half(v - static_cast<double>(__half2float(hi)));
 }
 
-// Transposed split outputs (the polar iteration's X^T operand): lane = row,
-// so for each column the warp's 32 consecutive rows are one contiguous
-// segment.  v = alpha*acc + diag*[row == col] (no accumulate with splits).
+// Epilogue of the polar-iteration GEMMs (GemmOut with split outputs, a
+// diagonal term or no C): v = alpha*acc + diag*[row == col] (+ C if
+// accumulate), stored to C (FP64) if present and as TF32 hi/lo pairs,
+// row-major and/or transposed.  It only stores (no loads unless it
+// accumulates), so the stores of one tile overlap the next tile's MMAs; the
+// transposed pairs are written by consecutive lanes (= consecutive rows)
+// and so coalesce; the row-major ones use 16-byte stores where aligned.
 template <int BNT, bool F16>
-__device__ __forceinline__ void store_transposed(const float* acc, const GemmOut& out, int gm, int n0) {
+__device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out, int gm, int n0) {
+  double* C = static_cast<double*>(out.C);
+  const long long crow = (long long)gm * out.ldm;
+  const bool full = n0 + BNT <= out.N;
+  const bool cvec = full && C && out.ldn == 1 && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) && out.ldm % 2 == 0;
+  // 4 split values per store: 16 bytes (tf32 pairs) or 8 bytes (fp16)
+  const bool rvec = full && out.rhi && ((reinterpret_cast<uintptr_t>(out.rhi) & 15) == 0) &&
+                    ((reinterpret_cast<uintptr_t>(out.rlo) & 15) == 0) && out.rld % 4 == 0;
 #pragma unroll
-  for (int c = 0; c < BNT; ++c) {
-    const int gn = n0 + c;
-    if (gn < out.N) {
-      const double v = static_cast<double>(out.alpha * acc[c]) + (gn == gm ? out.diag : 0.0);
-      const long long o = (long long)gn * out.tld + gm;
-      if constexpr (F16) {
-        __half h, l;
-        split2h(v, out.split_scale, h, l);
-        static_cast<__half*>(out.thi)[o] = h;
-        static_cast<__half*>(out.tlo)[o] = l;
+  for (int c = 0; c < BNT; c += 4) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = static_cast<double>(out.alpha * acc[c + j]) + (n0 + c + j == gm ? out.diag : 0.0);
+    if (C) {
+      if (cvec) {
+        double2* p = reinterpret_cast<double2*>(C + crow + n0 + c);
+        if (out.accumulate) {
+          const double2 a = p[0], b = p[1];
+          v[0] += a.x; v[1] += a.y; v[2] += b.x; v[3] += b.y;
+        }
+        p[0] = make_double2(v[0], v[1]);
+        p[1] = make_double2(v[2], v[3]);
       } else {
-        float h, l;
-        split2(v, h, l);
-        static_cast<float*>(out.thi)[o] = h;
-        static_cast<float*>(out.tlo)[o] = l;
-      }
-    }
-  }
-}
-
-// Row-major outputs of one warp's 32 rows through its 32 x 33 shared-memory
-// tile, 32 columns at a time: each lane deposits its row, then the warp
-// writes one row per step with consecutive lanes on consecutive columns, so
-// every store instruction covers one contiguous row segment (stored
-// directly, the 32 lanes would address 32 different rows; those scattered
-// stores took 10-18 us per tile).  The arithmetic is the direct form's:
-// alpha*acc in FP32, then widened, (+ diag, + C if accumulate), then split.
-template <int BNT, bool EXTRA, bool F16>
-__device__ __forceinline__ void store_rows_staged(const float* acc, const GemmOut& out, int row0, int n0, int lane,
-                                                  float* st) {
 #pragma unroll
-  for (int c0 = 0; c0 < BNT; c0 += 32) {
-#pragma unroll
-    for (int j = 0; j < 32; ++j) st[lane * STG_LD + j] = acc[c0 + j];
-    __syncwarp();
-    const int gn = n0 + c0 + lane;
-    const bool col_ok = gn < out.N;
-    for (int r = 0; r < 32; ++r) {
-      const int gm = row0 + r;
-      if (gm >= out.M) break;   // uniform across the warp
-      if (col_ok) {
-        const float a = out.alpha * st[r * STG_LD + lane];
-        const long long oc = (long long)gm * out.ldm + (long long)gn * out.ldn;
-        if constexpr (EXTRA) {
-          double v = static_cast<double>(a) + (gn == gm ? out.diag : 0.0);
-          if (out.C) {
-            double* pc = static_cast<double*>(out.C) + oc;
-            if (out.accumulate) v += *pc;
-            *pc = v;
+        for (int j = 0; j < 4; ++j) {
+          const int gn = n0 + c + j;
+          if (gn < out.N) {
+            const long long o = crow + (long long)gn * out.ldn;
+            if (out.accumulate) v[j] += C[o];
+            C[o] = v[j];
           }
-          if (out.rhi) {
-            const long long o = (long long)gm * out.rld + gn;
-            if constexpr (F16) {
-              __half h, l;
-              split2h(v, out.split_scale, h, l);
-              static_cast<__half*>(out.rhi)[o] = h;
-              static_cast<__half*>(out.rlo)[o] = l;
-            } else {
-              float h, l;
-              split2(v, h, l);
-              static_cast<float*>(out.rhi)[o] = h;
-              static_cast<float*>(out.rlo)[o] = l;
-            }
-          }
-        } else if (out.out_f64) {
-          double* C = static_cast<double*>(out.C);
-          C[oc] = out.accumulate ? C[oc] + static_cast<double>(a) : static_cast<double>(a);
-        } else {
-          float* C = static_cast<float*>(out.C);
-          C[oc] = out.accumulate ? C[oc] + a : a;
         }
       }
     }
-    __syncwarp();
+    if (out.rhi || out.thi) {
+      if constexpr (F16) {
+        __half h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) split2h(v[j], out.split_scale, h[j], l[j]);
+        if (out.rhi) {
+          __half* ph = static_cast<__half*>(out.rhi) + (long long)gm * out.rld + n0 + c;
+          __half* pl = static_cast<__half*>(out.rlo) + (long long)gm * out.rld + n0 + c;
+          if (rvec) {
+            __half2 h01 = __halves2half2(h[0], h[1]), h23 = __halves2half2(h[2], h[3]);
+            __half2 l01 = __halves2half2(l[0], l[1]), l23 = __halves2half2(l[2], l[3]);
+            uint2 uh, ul;
+            uh.x = *reinterpret_cast<uint32_t*>(&h01); uh.y = *reinterpret_cast<uint32_t*>(&h23);
+            ul.x = *reinterpret_cast<uint32_t*>(&l01); ul.y = *reinterpret_cast<uint32_t*>(&l23);
+            *reinterpret_cast<uint2*>(ph) = uh;
+            *reinterpret_cast<uint2*>(pl) = ul;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (n0 + c + j < out.N) {
+                ph[j] = h[j];
+                pl[j] = l[j];
+              }
+          }
+        }
+        if (out.thi) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + c + j;
+            if (gn < out.N) {
+              static_cast<__half*>(out.thi)[(long long)gn * out.tld + gm] = h[j];
+              static_cast<__half*>(out.tlo)[(long long)gn * out.tld + gm] = l[j];
+            }
+          }
+        }
+      } else {
+        float h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) split2(v[j], h[j], l[j]);
+        if (out.rhi) {
+          float* ph = static_cast<float*>(out.rhi) + (long long)gm * out.rld + n0 + c;
+          float* pl = static_cast<float*>(out.rlo) + (long long)gm * out.rld + n0 + c;
+          if (rvec) {
+            *reinterpret_cast<float4*>(ph) = make_float4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<float4*>(pl) = make_float4(l[0], l[1], l[2], l[3]);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (n0 + c + j < out.N) {
+                ph[j] = h[j];
+                pl[j] = l[j];
+              }
+          }
+        }
+        if (out.thi) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int gn = n0 + c + j;
+            if (gn < out.N) {
+              static_cast<float*>(out.thi)[(long long)gn * out.tld + gm] = h[j];
+              static_cast<float*>(out.tlo)[(long long)gn * out.tld + gm] = l[j];
+            }
+          }
+        }
+      }
+    }
   }
 }
 
@@ -194,8 +219,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   constexpr int NACC = (512 / ACC_COLS) < 4 ? (512 / ACC_COLS) : 4;   // TMEM ring of K-slice buffers
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  float* stg = reinterpret_cast<float*>(smem + STAGES * ST_BYTES);   // epilogue staging tiles
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES + STG_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * ST_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* acc_full = empty + STAGES;
   uint64_t* acc_empty = acc_full + NACC;
@@ -346,44 +370,74 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       }
       if (!ok) break;
       const int gm = m0 + row;
-      float* stw = stg + (warp - 2) * 32 * STG_LD;
       if constexpr (EXTRA) {
-        if (out.thi && gm < out.M) store_transposed<BNT, F16>(acc, out, gm, n0);
-        if (out.C || out.rhi) store_rows_staged<BNT, true, F16>(acc, out, m0 + q * 32, n0, lane, stw);
-      } else if (out.ldn == 1) {
-        store_rows_staged<BNT, false, F16>(acc, out, m0 + q * 32, n0, lane, stw);
-      } else if (gm < out.M) {
-        if (out.ldm == 1 && !out.out_f64 && !out.accumulate) {
-          // transposed FP32 overwrite (the matvec's X1): one coalesced
-          // 4-byte store per element across the warp's consecutive rows
-          float* pc = static_cast<float*>(out.C) + gm + (long long)n0 * out.ldn;
-          if (n0 + BNT <= out.N) {
+        if (gm < out.M) store_extra<BNT, F16>(acc, out, gm, n0);
+      } else {
+      // full-width tiles of row-contiguous outputs are written with 16-byte
+      // stores (4 floats / 2+2 doubles per step) instead of one element
+      const bool inrow = ok && gm < out.M;
+      // transposed FP32 overwrite (the matvec's X1): one coalesced 4-byte
+      // store per element across the warp's consecutive rows, no branches
+      const bool tstore = inrow && out.ldm == 1 && !out.out_f64 && !out.accumulate;
+      if (tstore) {
+        float* pc = static_cast<float*>(out.C) + gm + (long long)n0 * out.ldn;
+        if (n0 + BNT <= out.N) {
 #pragma unroll
-            for (int c = 0; c < BNT; ++c) pc[(long long)c * out.ldn] = out.alpha * acc[c];
-          } else {
-#pragma unroll
-            for (int c = 0; c < BNT; ++c)
-              if (n0 + c < out.N) pc[(long long)c * out.ldn] = out.alpha * acc[c];
-          }
+          for (int c = 0; c < BNT; ++c) pc[(long long)c * out.ldn] = out.alpha * acc[c];
         } else {
-          const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
-          for (int c = 0; c < BNT; ++c) {
-            const int gn = n0 + c;
-            if (gn < out.N) {
-              const float r = out.alpha * acc[c];
-              const long long o = rowoff + (long long)gn * out.ldn;
-              if (out.out_f64) {
-                double* C = static_cast<double*>(out.C);
-                C[o] = out.accumulate ? C[o] + (double)r : (double)r;
-              } else {
-                float* C = static_cast<float*>(out.C);
-                C[o] = out.accumulate ? C[o] + r : r;
+          for (int c = 0; c < BNT; ++c)
+            if (n0 + c < out.N) pc[(long long)c * out.ldn] = out.alpha * acc[c];
+        }
+      }
+      const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
+                       ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
+                       (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
+      if (inrow && !tstore) {
+        const long long rowoff = (long long)gm * out.ldm;
+#pragma unroll
+        for (int c = 0; c < BNT; c += 4) {
+          const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
+          const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
+          if (vec) {
+            if (out.out_f64) {
+              double2* p = reinterpret_cast<double2*>(static_cast<double*>(out.C) + rowoff + n0 + c);
+              double2 u = make_double2(r0, r1), v = make_double2(r2, r3);
+              if (out.accumulate) {
+                const double2 pu = p[0], pv = p[1];
+                u.x += pu.x; u.y += pu.y; v.x += pv.x; v.y += pv.y;
+              }
+              p[0] = u;
+              p[1] = v;
+            } else {
+              float4* p = reinterpret_cast<float4*>(static_cast<float*>(out.C) + rowoff + n0 + c);
+              float4 u = make_float4(r0, r1, r2, r3);
+              if (out.accumulate) {
+                const float4 o = *p;
+                u.x += o.x; u.y += o.y; u.z += o.z; u.w += o.w;
+              }
+              *p = u;
+            }
+          } else {
+            const float rr[4] = {r0, r1, r2, r3};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int gn = n0 + c + j;
+              if (gn < out.N) {
+                const long long o = rowoff + (long long)gn * out.ldn;
+                if (out.out_f64) {
+                  double* C = static_cast<double*>(out.C);
+                  C[o] = out.accumulate ? C[o] + (double)rr[j] : (double)rr[j];
+                } else {
+                  float* C = static_cast<float*>(out.C);
+                  C[o] = out.accumulate ? C[o] + rr[j] : rr[j];
+                }
               }
             }
           }
         }
       }
+    }
     }
   }
   tc_fence_before();
@@ -725,7 +779,6 @@ int gemm_split(const void* Ahi, const void* Alo, const void* Bhi, const void* Bl
   DMRG_TRY(make_map(&mal, Alo, M, Kp, BM, f16));
   const bool extra = out.rhi || out.thi || !out.C || out.diag != 0.0;
   if (extra && !out.out_f64) return DMRG_ERR_ARG;
-  if ((out.rhi || out.thi) && out.accumulate) return DMRG_ERR_ARG;   // split outputs hold alpha*acc + diag only
   auto launch = [&](const GemmCfg& c) -> int {
     return f16 ? gemm_launch_cfg<true>(c.bnt, c.merge, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s)
                : gemm_launch_cfg<false>(c.bnt, c.merge, extra, mah, mal, Bhi, Blo, M, N, Kp, c.group, out, err, s);
