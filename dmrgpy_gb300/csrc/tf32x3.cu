@@ -4,21 +4,29 @@
 // lo = tf32(x - hi); a product is formed from three TF32 MMAs,
 // A_hi.B_hi + A_hi.B_lo + A_lo.B_hi, accumulated in FP32 in TMEM (the
 // lo.lo term is below FP32 resolution and dropped).  That gives FP32-level
-// accuracy (~1e-7 relative) at tensor-core rate.
+// accuracy (~1e-7 relative) at tensor-core rate.  The same kernel runs FP16
+// pairs of power-of-two scaled operands (kind::f16, the same 22-bit split),
+// used by the polar iteration of the subspace truncation.
 //
-// GEMM kernel (C[M,N] = sum_k A[M,k] B[N,k], both operands K-major):
-//   warp 0   TMA producer: per K-slice of 32 fp32 (one 128-byte swizzle
-//            row) loads the A_hi, A_lo, B_hi, B_lo tiles into a shared
-//            memory stage (SWIZZLE_128B), signalling an mbarrier with the
-//            transaction byte count;
-//   warp 1   allocates TMEM, then one elected thread issues
-//            tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=BN, K=8), four
-//            K-steps x three products per stage, and tcgen05.commit's the
-//            stage back to the producer;
-//   warps 2-5 epilogue: wait for the final commit, tcgen05.ld the 128 x BN
-//            FP32 accumulator (each warp reads its 32-lane TMEM quarter) and
-//            store FP32 or FP64 with arbitrary output strides.
-// All mbarrier waits are bounded (DMRG_ERR_TIMEOUT is recorded on expiry).
+// GEMM kernel (C[M,N] = sum_k A[M,k] B[N,k], both operands K-major),
+// persistent: one CTA per SM walks the output tiles b, b + gridDim.x, ...
+//   warp 0   TMA producer: per stage (one 128-byte swizzle row of K: 32 tf32
+//            or 64 fp16) loads the A_hi, A_lo, B_hi, B_lo tiles into a
+//            shared-memory ring (SWIZZLE_128B), signalling an mbarrier with
+//            the transaction byte count;
+//   warp 1   allocates TMEM, then one thread issues tcgen05.mma.cta_group::1
+//            (kind::tf32 K=8 or kind::f16 K=16; M=128, N=BNT or, merged,
+//            one N=2 BNT MMA for A_hi.[B_hi; B_lo]) into a ring of TMEM
+//            buffers, one per 32-wide K run, and tcgen05.commit's the stage
+//            back to the producer and each buffer to the epilogue;
+//   warps 2-5 epilogue: each thread owns one output row (its warp's 32-lane
+//            TMEM quarter), adds every K run's buffer into FP32 registers,
+//            and after the tile's last run stores FP32/FP64 with arbitrary
+//            strides, or (polar iteration) FP64 plus the TF32/FP16 operand
+//            pairs of the next GEMM.
+// The stage and TMEM rings run on across tiles, so a tile's stores overlap
+// the next tile's loads and MMAs.  All mbarrier waits are bounded
+// (DMRG_ERR_TIMEOUT is recorded on expiry).
 //
 // Around the GEMMs: split kernels that produce the K-padded hi/lo operand
 // arrays (optionally transposing), and the MPO-step kernel that contracts
