@@ -4,20 +4,21 @@
 // cores, one of them a Gram matrix accurate to ~1e-13 (exact digit products,
 // gram.cu).
 //
-//   keep the left factor (absorb 0):
-//     Y = theta^T X      X: m x k start basis (the current left site tensor)
-//     W = orth(Y)        n x k
-//     Z = theta W        m x k
-//     Q = orth(Z)        left factor  (m x k, orthonormal columns)
-//     C = Q^T theta      right factor (k x n)
+//   keep the left factor (absorb 0), starting from X = the tensor across the
+//   bond (k x n, orthonormal rows in a right-canonical MPS):
+//     W = orth(X^T)      n x k
+//     Z = theta W        m x k     (iters times, with W = orth(theta^T Q)
+//     Q = orth(Z)        m x k      between two rounds)
+//     C = Q^T theta      right factor (k x n); left factor Q
 //   keep the right factor (absorb 1): the same on theta^T, returning
 //     left = theta Q (m x k) and right = Q^T (k x n, orthonormal rows).
+// The products with theta are split-TF32.
 //
 // orth() is the polar factor of the block by Newton-Schulz iterations, which
-// are GEMMs only (split-TF32 on the tensor cores); the final left/right basis
-// gets one more correction from a near-FP64 Gram matrix so that it is
-// orthonormal to ~1e-11 (a basis that is only FP32-orthonormal lets the norm
-// environment drift along the chain).
+// are GEMMs only (FP16-split operand pairs on the tensor cores); the final
+// left/right basis gets one more correction from the near-FP64 Gram matrix
+// so that it is orthonormal to ~1e-13 (a basis that is only FP32-orthonormal
+// lets the norm environment drift along the chain).
 #include <cuda_fp16.h>
 
 #include <cmath>
