@@ -137,6 +137,28 @@ def cpu_bond_sample(L, Wi, Wj, R, theta, Lnext_A, k_lanczos, maxdim):
     return {"t_matvec": t_mv, "t_svd": t_svd, "t_env": t_env, "t_bond": t_bond}
 
 
+def max_over_ranks(value, dist, device):
+    """The largest of the ranks' values (the job's time is that of its
+    slowest replica); the value itself in a single process."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value, dist, device):
+    """The sum of the ranks' values (the work of all replicas: they run
+    different seeds, so their Lanczos counts differ)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def host_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -238,13 +260,10 @@ def run_gpu(args):
     launches = lib.dmrg_kernel_launches() - l0
     clk = clocks.stop()
     t_dev = ev0.elapsed_time(ev1) / 1e3
-    elapsed = max(t_dev, 0.0)
-    if dist:
-        tt = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    dev = "cuda:%d" % local
+    elapsed = max_over_ranks(max(t_dev, 0.0), dist, dev)
     st = eng.stats
-    flops = st.matvec_flops * world
+    flops = sum_over_ranks(st.matvec_flops, dist, dev)
     value = flops / elapsed / 1e12
     iters = [r["iters"] for r in st.records]
     chis = [max(r["chil"], r["chir"]) for r in st.records]

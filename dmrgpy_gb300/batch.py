@@ -31,6 +31,25 @@ def _ptrs(tensors):
     return (ctypes.c_void_p * len(tensors))(*[t.data_ptr() for t in tensors])
 
 
+def partition_chains(costs, nparts):
+    """Assigns independent chains to nparts ranks (GPUs) so that their summed
+    costs balance, e.g. chi^3 d^2 w per chain for the matvec-dominated
+    sweep: longest first, each chain to the rank with the least cost so far
+    (ties to the lower rank).  Deterministic, so every rank computes the same
+    assignment without communication; the ranks then sweep their shares with
+    no collective.  Returns one ascending list of chain indices per rank."""
+    if nparts < 1:
+        raise ValueError("nparts must be >= 1")
+    order = sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i))
+    load = [0.0] * nparts
+    parts = [[] for _ in range(nparts)]
+    for i in order:
+        r = min(range(nparts), key=lambda j: (load[j], j))
+        parts[r].append(i)
+        load[r] += float(costs[i])
+    return [sorted(p) for p in parts]
+
+
 class BatchEngine:
     """Lock-step sweeps of len(Ws) chains.
 
