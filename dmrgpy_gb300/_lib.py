@@ -85,6 +85,7 @@ SIGNATURES = [
                                        c_void_p, P_double, c_void_p, c_size_t, c_void_p]),
     ("dmrg_gram_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
     ("dmrg_gram", c_int, [c_int, c_int, c_int, c_void_p, ctypes.c_longlong, c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_wait_timeout_probe", c_int, [c_void_p, c_size_t, c_void_p]),
     ("dmrg_gemm", c_int, [c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                           c_void_p]),
     ("dmrg_gemm_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int, c_int]),

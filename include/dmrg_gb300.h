@@ -301,6 +301,14 @@ size_t dmrg_gram_workspace_bytes(int method, int m, int k);
 int dmrg_gram(int method, int m, int k, const void* X, long long ld, void* G, void* work, size_t work_bytes,
               void* stream);
 
+/* ---- bounded-wait probe ----------------------------------------------------
+ * No reference counterpart: launches one kernel whose mbarrier wait nothing
+ * completes, with the bounded wait of the tcgen05 kernels (~2 s), and
+ * returns the status it recorded, DMRG_ERR_TIMEOUT; the device stays
+ * usable.  Exercises the timeout path without a fault.  work: >= 256 bytes
+ * of device memory.  Synchronises the stream. */
+int dmrg_wait_timeout_probe(void* work, size_t work_bytes, void* stream);
+
 /* ---- dense contraction ---------------------------------------------------- */
 size_t dmrg_gemm_workspace_bytes(int dtype, int precision, int m, int k, int n);
 /* C (m x n) = A (m x k) . B (k x n), all row-major.  Used for the two-site
