@@ -104,14 +104,20 @@ def measured_peaks():
         return 1900.0, 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per matvec launch from the committed ncu summary, if any."""
+def profile_summary():
+    """DRAM bytes per matvec and the per-kernel ncu figures (time share,
+    tensor-pipe utilisation) from the committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", "heff_tf32x3_chi1024.json")
     try:
         with open(p) as f:
-            return json.load(f).get("dram_bytes_per_matvec")
+            d = json.load(f)
     except Exception:
-        return None
+        return None, None
+    ks = d.get("kernels") or []
+    tot = sum(k.get("us", 0.0) for k in ks) or 1.0
+    kernels = [{"kernel": k.get("kernel"), "us": k.get("us"), "share": k.get("us", 0.0) / tot,
+                "tensor_pipe_pct": k.get("tensor"), "dram_pct": k.get("dram")} for k in ks]
+    return d.get("dram_bytes_per_matvec"), kernels
 
 
 # ---------------------------------------------------------------- CPU oracle sample
@@ -299,8 +305,9 @@ def run_gpu(args):
     t_mv = s0.elapsed_time(s1) / 1e3 / reps
     bf16, hbm, peak_kind = measured_peaks()
     achieved = f_mv / t_mv / 1e12
+    traffic, ncu_kernels = profile_summary()
     roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s", "frac": achieved / bf16,
-            "traffic": profile_traffic(), "peak_source": peak_kind,
+            "traffic": traffic, "peak_source": peak_kind, "ncu_kernels": ncu_kernels,
             "kernel": "two-site H_eff matvec per Krylov iteration (split-TF32 tcgen05 GEMMs + MPO step), "
                       "chi=1024 d=3 w=5",
             "flops_per_launch": f_mv, "launch_s": t_mv,
