@@ -18,6 +18,7 @@ DMRG_ERR_NAN = 4
 DMRG_ERR_NOCONV = 5
 DMRG_ERR_TIMEOUT = 6
 DMRG_ERR_UNSUPPORTED = 7
+DMRG_ERR_PRECISION = 8
 
 # size of the fixed device array behind dmrg_heff_apply_noalloc
 # (DMRG_NOALLOC_SCRATCH_BYTES in include/dmrg_gb300.h)
@@ -83,6 +84,13 @@ SIGNATURES = [
     ("dmrg_subspace_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
     ("dmrg_subspace_truncate", c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_void_p,
                                        c_void_p, P_double, c_void_p, c_size_t, c_void_p]),
+    ("dmrg_subspace_truncate_ex_workspace_bytes", c_size_t, [c_int, c_int, c_int, c_int]),
+    ("dmrg_subspace_truncate_ex", c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int, c_int, c_int,
+                                          c_double, c_int, c_void_p, c_void_p, P_double, P_int, P_double, c_void_p,
+                                          c_size_t, c_void_p]),
+    ("dmrg_syev_workspace_bytes", c_size_t, [c_int]),
+    ("dmrg_syev", c_int, [c_int, c_void_p, ctypes.c_longlong, P_double, c_void_p, ctypes.c_longlong, P_int,
+                          c_void_p, c_size_t, c_void_p]),
     ("dmrg_gram_workspace_bytes", c_size_t, [c_int, c_int, c_int]),
     ("dmrg_gram", c_int, [c_int, c_int, c_int, c_void_p, ctypes.c_longlong, c_void_p, c_void_p, c_size_t, c_void_p]),
     ("dmrg_wait_timeout_probe", c_int, [c_void_p, c_size_t, c_void_p]),

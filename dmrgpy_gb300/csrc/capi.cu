@@ -405,10 +405,36 @@ void keep_rule(const double* s, int n, double cutoff, int maxdim, int mindim, in
 
 namespace {
 
+// Real matrices with min(m, n) >= 16 take the Gram-matrix route of
+// pyitensor/svd.py:108-151 (gramtrunc.cu) when the Gram matrix of the kept
+// side is at most twice the smaller side and at most 4096; everything else
+// (the reference's exact-SVD cases, complex matrices, strongly rectangular
+// shapes) the one-sided Jacobi SVD.
+bool gram_route(int dtype, int m, int n, int absorb) {
+  if (dtype != DMRG_REAL64) return false;
+  const int c = std::min(m, n);
+  if (c < 16) return false;
+  const int ck = absorb == 0 ? m : absorb == 1 ? n : c;
+  return ck <= 2 * c && ck <= 4096;
+}
+
+size_t svd_total_bytes(int dtype, int m, int n, int absorb) {
+  size_t b = svd_work_bytes(dtype, m, n);
+  if (gram_route(dtype, m, n, absorb)) b = std::max(b, gram_truncate_workspace_bytes(m, n, absorb));
+  return b;
+}
+
 template <typename T>
 int svd_impl(int m, int n, const T* M, double cutoff, int maxdim, int mindim, int absorb, T* lo, T* ro, double* svals,
              int* keep, double* disc, void* work, size_t work_bytes, cudaStream_t s) {
-  if (svd_work_bytes(sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64, m, n) > work_bytes) return DMRG_ERR_WORKSPACE;
+  const int dtype = sizeof(T) == 16 ? DMRG_COMPLEX128 : DMRG_REAL64;
+  if (svd_total_bytes(dtype, m, n, absorb) > work_bytes) return DMRG_ERR_WORKSPACE;
+  if (gram_route(dtype, m, n, absorb)) {
+    const int st = gram_truncate(m, n, reinterpret_cast<const double*>(M), cutoff, maxdim, mindim, absorb,
+                                 reinterpret_cast<double*>(lo), reinterpret_cast<double*>(ro), svals, keep, disc,
+                                 nullptr, work, work_bytes, s);
+    if (st != GRAM_FALLBACK) return st;
+  }
   const int c = std::min(m, n);
   std::vector<double> sv(c);
   int sweeps = 0;
@@ -447,6 +473,7 @@ const char* dmrg_status_string(int status) {
     case DMRG_ERR_NOCONV: return "iterative solver did not converge";
     case DMRG_ERR_TIMEOUT: return "bounded device wait timed out";
     case DMRG_ERR_UNSUPPORTED: return "unsupported combination";
+    case DMRG_ERR_PRECISION: return "split-TF32 weights cannot resolve the cutoff; use the FP64 route";
     default: return "unknown status";
   }
 }
@@ -562,7 +589,9 @@ int dmrg_krylov_expm(const dmrg_heff_t* op, void* x, double coeff_re, double coe
 
 size_t dmrg_svd_workspace_bytes(int dtype, int m, int n) {
   if (m <= 0 || n <= 0) return 0;
-  return svd_work_bytes(dtype, m, n);
+  size_t b = 0;
+  for (int absorb = 0; absorb < 3; ++absorb) b = std::max(b, svd_total_bytes(dtype, m, n, absorb));
+  return b;
 }
 
 int dmrg_svd_truncate(int dtype, int m, int n, const void* M, double cutoff, int maxdim, int mindim, int absorb,
@@ -647,6 +676,89 @@ int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* s
   return subspace_truncate(m, n, k, static_cast<const double*>(theta), static_cast<const double*>(start), kstart,
                            absorb, iters, static_cast<double*>(left_out), static_cast<double*>(right_out), discarded,
                            work, work_bytes, static_cast<cudaStream_t>(stream));
+}
+
+size_t dmrg_syev_workspace_bytes(int n) { return n > 0 ? syev_jacobi_workspace_bytes(n) : 0; }
+
+int dmrg_syev(int n, const void* A, long long lda, double* w, void* V, long long ldv, int* sweeps, void* work,
+              size_t work_bytes, void* stream) {
+  if (n <= 0 || !A || lda < n || !w || (V && ldv < n)) return DMRG_ERR_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DMRG_TRY(syev_jacobi(n, static_cast<const double*>(A), lda, w, 40, sweeps, work, work_bytes, s));
+  if (V) {
+    DMRG_TRY(syev_vectors(n, n, static_cast<double*>(V), ldv, 0, work, s));
+    DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+  }
+  return DMRG_OK;
+}
+
+size_t dmrg_subspace_truncate_ex_workspace_bytes(int precision, int m, int n, int k) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  if (precision == DMRG_PREC_FP64) return rr_truncate_workspace_bytes(m, n, k);
+  // the residual check of a positive cutoff reuses the Ritz scratch:
+  // theta - lo ro (m x n) plus the split operands of that product
+  const size_t ritz = std::max(subspace_ritz_workspace_bytes(m, n, k),
+                               align_up(sizeof(double) * (size_t)m * n) + tf32x3_gemm_ex_workspace_bytes(m, n, k));
+  return subspace_workspace_bytes(m, n, k) + ritz + align_up(64);
+}
+
+int dmrg_subspace_truncate_ex(int precision, int m, int n, int k, const void* theta, const void* start, int kstart,
+                              int absorb, int iters, double cutoff, int mindim, void* left_out, void* right_out,
+                              double* svals, int* keep, double* discarded, void* work, size_t work_bytes,
+                              void* stream) {
+  if (m <= 0 || n <= 0 || k <= 0 || k > std::min(m, n) || !theta || !left_out || !right_out || !keep ||
+      (kstart > 0 && !start) || (absorb != 0 && absorb != 1) || (precision == DMRG_PREC_FP64 && !svals))
+    return DMRG_ERR_ARG;
+  if (precision != DMRG_PREC_FP64 && precision != DMRG_PREC_TF32X3) return DMRG_ERR_ARG;
+  if (!work || dmrg_subspace_truncate_ex_workspace_bytes(precision, m, n, k) > work_bytes) return DMRG_ERR_WORKSPACE;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const double* th = static_cast<const double*>(theta);
+  double* lo = static_cast<double*>(left_out);
+  double* ro = static_cast<double*>(right_out);
+  double disc = 0.0;
+  if (precision == DMRG_PREC_FP64) {
+    int nv = 0;
+    DMRG_TRY(rr_truncate(m, n, k, th, static_cast<const double*>(start), kstart, absorb, iters, cutoff, mindim, lo,
+                         ro, svals, &nv, keep, &disc, work, work_bytes, s));
+    for (int i = nv; i < k; ++i) svals[i] = 0.0;
+  } else {
+    const size_t sb = subspace_workspace_bytes(m, n, k);
+    char* base = static_cast<char*>(work);
+    double* tot = reinterpret_cast<double*>(base + sb);
+    void* rw = base + sb + align_up(64);
+    DMRG_TRY(subspace_truncate(m, n, k, th, static_cast<const double*>(start), kstart, absorb, iters, lo, ro, &disc,
+                               work, sb, s));
+    if (cutoff > 0.0) {
+      // the weight outside the kept space as |theta - lo ro|^2: the
+      // split-TF32 error of the factors (~5e-7 |theta|) enters it squared
+      // plus a cross term, whereas |theta|^2 - |C|^2 carries it linearly
+      double* res = static_cast<double*>(rw);
+      int* err = reinterpret_cast<int*>(tot + 2);
+      DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+      DMRG_CUDA_TRY(cudaMemcpyAsync(res, th, sizeof(double) * (size_t)m * n, cudaMemcpyDeviceToDevice, s));
+      DMRG_TRY(tf32x3_gemm_ex(0, 0, m, n, k, -1.f, lo, k, ro, n, 1, res, n,
+                              static_cast<char*>(rw) + align_up(sizeof(double) * (size_t)m * n), err, s));
+      DMRG_TRY(sumsq_dev(th, (long long)m * n, tot, s));
+      DMRG_TRY(sumsq_dev(res, (long long)m * n, tot + 1, s));
+      int e = 0;
+      double h[2] = {0.0, 0.0};
+      DMRG_CUDA_TRY(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+      DMRG_CUDA_TRY(cudaMemcpyAsync(h, tot, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      DMRG_CUDA_TRY(cudaStreamSynchronize(s));
+      if (e != 0) return e;
+      const double rem = h[0] > 0.0 ? h[1] / h[0] : 0.0;
+      // keep = k is the rule's answer when the weight beyond the kept space
+      // exceeds the cutoff (no kept direction may then be dropped); decide it
+      // only when that holds beyond the estimate's own error, else leave
+      // the bond to the FP64 route
+      if (!(rem - (1e-12 + 2e-6 * std::sqrt(rem)) > cutoff)) return DMRG_ERR_PRECISION;
+      disc = rem;
+    }
+    *keep = k;
+    if (svals) DMRG_TRY(subspace_ritz(m, n, k, absorb, lo, ro, svals, rw, work_bytes - sb - align_up(64), s));
+  }
+  if (discarded) *discarded = disc;
+  return DMRG_OK;
 }
 
 }  // extern "C"

@@ -54,6 +54,31 @@ int hestenes_batch_output(int nprob, const int* m, const int* n, const int* keep
 bool tridiag_eig(int n, std::vector<double>& d, std::vector<double> e, std::vector<double>* z);
 int lowest_ritz(const std::vector<double>& al, const std::vector<double>& be, double* ev, std::vector<double>* vec);
 void keep_rule(const double* s, int n, double cutoff, int maxdim, int mindim, int* keep, double* disc);
+void keep_rule_partial(const double* lam, int k, int c, double total, double cutoff, int maxdim, int mindim,
+                       double rem, int* keep, double* disc);
+
+// symmetric eigendecomposition by blocked Jacobi (syev.cu): eigenvalues to
+// the host (descending), eigenvectors gathered afterwards from the workspace
+size_t syev_jacobi_workspace_bytes(int n);
+int syev_jacobi(int n, const double* A, long long lda, double* w, int max_sweeps, int* sweeps, void* work,
+                size_t work_bytes, cudaStream_t s, int fp32 = 0);
+int syev_vectors(int n, int ncols, double* out, long long ldo, int transposed, void* work, cudaStream_t s,
+                 int fp32 = 0);
+
+// Gram-matrix truncation (gramtrunc.cu)
+constexpr int GRAM_FALLBACK = 100;   // internal: use the exact SVD instead
+int sumsq_dev(const double* x, long long n, double* out, cudaStream_t s);
+size_t gram_truncate_workspace_bytes(int m, int n, int absorb);
+int gram_truncate(int m, int n, const double* M, double cutoff, int maxdim, int mindim, int absorb, double* lo,
+                  double* ro, double* svals, int* keep, double* disc, int* sweeps, void* work, size_t work_bytes,
+                  cudaStream_t s);
+size_t rr_truncate_workspace_bytes(int m, int n, int k);
+int rr_truncate(int m, int n, int k, const double* theta, const double* X, int kx, int absorb, int iters,
+                double cutoff, int mindim, double* lo, double* ro, double* svals, int* nvals, int* keep, double* disc,
+                void* work, size_t work_bytes, cudaStream_t s);
+size_t subspace_ritz_workspace_bytes(int m, int n, int k);
+int subspace_ritz(int m, int n, int k, int absorb, double* lo, double* ro, double* svals, void* work,
+                  size_t work_bytes, cudaStream_t s);
 
 // vector ops
 template <typename T> int vaxpy2(T* y, const T* x1, const double* a1, const T* x2, const double* a2, long long n, cudaStream_t s);

@@ -21,8 +21,11 @@ LANCZOS_TOL = 1e-12          # pyitensor/dmrg.py:95
 # relative test applies; the bias is removed by the FP64 energy refinement.
 LANCZOS_TOL_TF32 = 1e-12
 TF32_MIN_CHI = 32            # bonds with a smaller chi stay on the FP64 path
-# split-TF32 sweeps with a maxdim-bound truncation (cutoff <= 0) factorise
-# theta by warm-started subspace iteration once min(m, n) reaches this size
+# bonds where maxdim binds factorise theta by warm-started subspace
+# iteration plus Rayleigh-Ritz once min(m, n) reaches this size (split-TF32
+# products in tf32x3 sweeps, FP64 products in fp64 sweeps and on every
+# split-TF32 bond where the cutoff may bind); smaller bonds take the full
+# Gram-matrix route of dmrg_svd_truncate
 SUBSPACE_MIN_DIM = 256
 LANCZOS_NITER_FLOOR = 200    # pyitensor/dmrg.py:315-330
 KRYLOV_ERRGOAL = 1e-10       # pyitensor/tdvp.py:79
@@ -57,6 +60,7 @@ class SweepStats:
         self.t = {"lanczos": 0.0, "svd": 0.0, "env": 0.0, "merge": 0.0}
         self.matvecs = 0
         self.matvec_flops = 0.0
+        self.fp64_truncations = 0   # split-TF32 bonds whose cutoff the FP64 route decided
 
     def add(self, **kw):
         self.records.append(kw)
@@ -94,6 +98,14 @@ class Engine:
         self.stats = SweepStats()
         self._renv = None  # right environments valid for the current MPS (after a RL pass)
         self.subspace_iters = 1     # subspace iterations per fixed-rank truncation
+        # optional callable(theta (m x n device matrix), cutoff, maxdim, keep,
+        # discarded) run after every bond truncation (tests inspect the
+        # two-site tensors of a sweep with it)
+        self.theta_hook = None
+        self.last_spectrum = None
+        # split-TF32 subspace truncations also return the Ritz values of the
+        # kept problem (an FP32 Jacobi per bond); off in sweeps by default
+        self.want_spectra = False
         self.lanczos_tol_tf32 = LANCZOS_TOL_TF32
 
     # ------------------------------------------------------------ plumbing
@@ -229,30 +241,52 @@ class Engine:
         k = keep.value
         return lo[:m * k].view(m, k), ro[:k * n].view(k, n), s, k, disc.value
 
-    def subspace_split(self, M2, k, start, kstart, absorb):
-        """Fixed-rank factorisation of a 2-D device matrix by warm-started
-        subspace iteration (split-TF32): -> (left, right, None, k, disc)."""
+    def subspace_split(self, M2, k, start, kstart, absorb, cutoff=0.0, mindim=1, prec=None):
+        """Truncation of a 2-D device matrix to at most k vectors by
+        warm-started subspace iteration plus Rayleigh-Ritz, with the cutoff
+        rule: -> (left, right, s, keep, disc).  prec: the engine's precision
+        by default; split-TF32 raises DmrgError(DMRG_ERR_PRECISION) where
+        its weights cannot decide the cutoff.  s holds the singular-value
+        estimates (FP64 route) or, with want_spectra, the FP32-accurate
+        Ritz values (split-TF32 route); else None."""
         torch = _torch()
         m, n = M2.shape
-        lo = torch.empty((m, k), dtype=self.tdtype, device=self.device)
-        ro = torch.empty((k, n), dtype=self.tdtype, device=self.device)
+        if prec is None:
+            prec = self.prec if self.prec == _lib.PREC_TF32X3 else _lib.PREC_FP64
+        lo = torch.empty(m * k, dtype=self.tdtype, device=self.device)
+        ro = torch.empty(k * n, dtype=self.tdtype, device=self.device)
         disc = ctypes.c_double(0.0)
-        need = self.lib.dmrg_subspace_workspace_bytes(m, n, k)
+        keep = ctypes.c_int(0)
+        want = prec == _lib.PREC_FP64 or self.want_spectra
+        s = np.zeros(k, dtype=np.float64) if want else None
+        need = self.lib.dmrg_subspace_truncate_ex_workspace_bytes(prec, m, n, k)
         ptr, size = self.ws.get(need)
-        st = self.lib.dmrg_subspace_truncate(m, n, k, M2.data_ptr(), start.data_ptr() if start is not None else None,
-                                             int(kstart), int(absorb), int(self.subspace_iters),
-                                             lo.data_ptr(), ro.data_ptr(),
-                                             ctypes.byref(disc), ptr, size, self.stream)
-        _lib.check("dmrg_subspace_truncate", st)
-        return lo, ro, None, k, disc.value
+        st = self.lib.dmrg_subspace_truncate_ex(prec, m, n, k, M2.data_ptr(),
+                                                start.data_ptr() if start is not None else None,
+                                                int(kstart), int(absorb), int(self.subspace_iters), float(cutoff),
+                                                int(mindim), lo.data_ptr(), ro.data_ptr(),
+                                                s.ctypes.data_as(_lib.P_double) if s is not None else None,
+                                                ctypes.byref(keep), ctypes.byref(disc), ptr, size, self.stream)
+        _lib.check("dmrg_subspace_truncate_ex", st)
+        kp = keep.value
+        return lo[:m * kp].view(m, kp), ro[:kp * n].view(kp, n), s, kp, disc.value
 
     def use_subspace(self, m, n, cutoff, maxdim):
-        """Split-TF32 sweeps with a maxdim-bound truncation use the fixed-rank
-        path: subspace iteration for large bonds, and for any size when the
-        kept rank is the full min(m, n) (then the subspace is exact)."""
+        """Real sweeps whose truncation is bound by maxdim on a large bond use
+        the subspace route (split-TF32 or FP64 products by the engine's
+        precision)."""
+        if not (self.real and maxdim and maxdim > 0):
+            return False
+        return min(m, n) >= SUBSPACE_MIN_DIM and maxdim < min(m, n)
+
+    def use_identity_split(self, m, n, cutoff, maxdim, absorb):
+        """Split-TF32 sweeps that keep the whole kept side with no cutoff:
+        the identity is an exact orthonormal basis and theta the other
+        factor, so nothing is factorised."""
         if not (self.prec == _lib.PREC_TF32X3 and self.real and cutoff <= 0.0 and maxdim and maxdim > 0):
             return False
-        return min(m, n) >= SUBSPACE_MIN_DIM or min(maxdim, m, n) == min(m, n)
+        rank = min(maxdim, m, n)
+        return (absorb == 0 and rank == m) or (absorb == 1 and rank == n)
 
     def env_left(self, L, W, A, fp64=False):
         torch = _torch()
@@ -418,7 +452,7 @@ class Engine:
         cl, d1, d2, cr = theta.shape
         m, n = cl * d1, d2 * cr
         rank = min(maxdim, m, n) if maxdim and maxdim > 0 else min(m, n)
-        if self.use_subspace(m, n, cutoff, maxdim) and ((absorb == 0 and rank == m) or (absorb == 1 and rank == n)):
+        if self.use_identity_split(m, n, cutoff, maxdim, absorb):
             # nothing to truncate on the kept side: the identity is an exact
             # orthonormal basis of it and theta itself the other factor
             eye = torch.eye(rank, dtype=self.tdtype, device=self.device)
@@ -438,15 +472,26 @@ class Engine:
                 kx = min(start.shape[1], rank)
                 start = start[:, :kx].contiguous()
             try:
-                lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb)
+                try:
+                    lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb, cutoff)
+                except _lib.DmrgError as ex:
+                    if ex.status != _lib.DMRG_ERR_PRECISION:
+                        raise
+                    # the cutoff may bind here: the FP64 route decides it
+                    self.stats.fp64_truncations += 1
+                    lo, ro, s, keep, disc = self.subspace_split(theta.view(m, n), rank, start, kx, absorb, cutoff,
+                                                                prec=_lib.PREC_FP64)
             except _lib.DmrgError as ex:
                 if ex.status != _lib.DMRG_ERR_NOCONV:
                     raise
-                # the polar iteration did not converge: exact FP64 truncation
-                lo, ro, s, keep, disc = self.svd(theta.view(m, n), 0.0, rank, 1, absorb)
+                # the basis could not be made orthonormal: the full FP64
+                # truncation
+                lo, ro, s, keep, disc = self.svd(theta.view(m, n), cutoff, maxdim, 1, absorb)
         else:
             lo, ro, s, keep, disc = self.svd(theta.view(m, n), cutoff, maxdim, 1, absorb)
         t3 = time.perf_counter()
+        if self.theta_hook is not None:
+            self.theta_hook(theta.view(m, n), cutoff, maxdim, keep, disc)
         st = self.stats
         st.t["merge"] += t1 - t0
         st.t["lanczos"] += t2 - t1
@@ -456,6 +501,7 @@ class Engine:
                                                     not self.real)
         if record:
             st.add(energy=energy, iters=iters, keep=keep, disc=disc, chil=cl, chir=cr)
+        self.last_spectrum = None if s is None else np.asarray(s[:keep], dtype=np.float64).copy()
         return energy, lo.view(cl, d1, keep), ro.view(keep, d2, cr), s, keep, disc
 
     def sweep(self, A, maxdim, cutoff, niter=2, record=False):

@@ -37,6 +37,8 @@ extern "C" {
 #define DMRG_ERR_NOCONV      5  /* an iterative eigensolver hit its sweep limit */
 #define DMRG_ERR_TIMEOUT     6  /* a bounded device-side wait gave up */
 #define DMRG_ERR_UNSUPPORTED 7  /* combination not built (e.g. complex + TF32x3) */
+#define DMRG_ERR_PRECISION   8  /* a split-TF32 estimate cannot decide what was asked
+                                   (callers repeat the step in FP64) */
 
 /* ---- element types and contraction precisions ------------------------ */
 #define DMRG_REAL64      0
@@ -182,13 +184,23 @@ int dmrg_krylov_expm(const dmrg_heff_t* op, void* x, double coeff_re, double coe
 
 /* ---- truncated factorisation --------------------------------------------- */
 size_t dmrg_svd_workspace_bytes(int dtype, int m, int n);
-/* Truncated SVD of the row-major m x n matrix M by one-sided (Hestenes)
- * Jacobi in FP64 on the min(m,n) columns of M^H or M, followed by the
- * cutoff/maxdim/mindim rule of pyitensor/svd.py:32-68.  The one-sided form
- * keeps small singular values to high relative accuracy, so it covers both
- * the Gram-matrix route of the reference and its exact-SVD fallback
- * (pyitensor/svd.py:108-151).  Replaces pyitensor/svd.py:108-195
- * (_svd_truncated, svd) as used by pyitensor/dmrg.py:336-352.
+/* Truncated SVD of the row-major m x n matrix M followed by the
+ * cutoff/maxdim/mindim rule of pyitensor/svd.py:32-68, in FP64.  Two routes,
+ * chosen like the reference's (pyitensor/svd.py:108-151):
+ *  - real M with min(m,n) >= 16 (and a kept side of at most 2 min(m,n) and
+ *    4096): the Gram-matrix route -- the FP64 Gram matrix of the side the
+ *    caller keeps orthonormal (M M^T for absorb 0, M^T M for absorb 1, the
+ *    smaller side for absorb 2), its eigendecomposition by blocked Jacobi
+ *    (dmrg_syev), singular values as square roots of the eigenvalues, the
+ *    kept eigenvectors as the orthonormal factor and one FP64 product for
+ *    the other (absorb 2 divides by S and, like svd.py:139, falls back to
+ *    the exact SVD when the smallest kept value is below 1e-7 of the
+ *    largest);
+ *  - otherwise one-sided (Hestenes) Jacobi on the min(m,n) columns of M^H
+ *    or M (the reference's np.linalg.svd cases), which keeps small singular
+ *    values to high relative accuracy.
+ * Replaces pyitensor/svd.py:108-195 (_svd_truncated, svd) as used by
+ * pyitensor/dmrg.py:336-352.
  *   absorb = 0: left_out = U (m x keep), right_out = S.Vh (keep x n)
  *   absorb = 1: left_out = U.S (m x keep), right_out = Vh (keep x n)
  *   absorb = 2: left_out = U, right_out = Vh (S only in svals)
@@ -227,6 +239,58 @@ size_t dmrg_subspace_workspace_bytes(int m, int n, int k);
 int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* start, int kstart, int absorb,
                            int iters, void* left_out, void* right_out, double* discarded,
                            void* work, size_t work_bytes, void* stream);
+
+/* Truncation of a large two-site tensor to at most k vectors by subspace
+ * iteration plus Rayleigh-Ritz with the cutoff/mindim rule of
+ * pyitensor/svd.py:32-68 (maxdim = k): the maxdim-bound case of
+ * pyitensor/svd.py:108-151 (Gram route) at bond dimensions where the full
+ * eigenproblem of the min(m,n)-sized Gram matrix is not needed.
+ * start/kstart/absorb/iters as dmrg_subspace_truncate.
+ *   DMRG_PREC_FP64:   every product FP64: Z = theta W from the start basis,
+ *                     Ritz pairs of theta^T theta on span(W) from the k x k
+ *                     FP64 Gram Z^T Z (dmrg_syev), kept basis
+ *                     U = Z E Lambda^(-1/2) made orthonormal to 1e-13 (weak
+ *                     directions below a cutoff-dependent fraction of the
+ *                     largest Ritz value replaced by an orthonormal
+ *                     completion), C = U^T theta; the rule runs on the
+ *                     weights |C_j|^2 with the rest of |theta|^2 as forced
+ *                     drops, and where it keeps fewer than k the subspace
+ *                     gets up to two more iterations and the final count
+ *                     comes from the Ritz values of theta theta^T on the
+ *                     kept space.  svals (host, k) receives the
+ *                     singular-value estimates.
+ *   DMRG_PREC_TF32X3: the basis of dmrg_subspace_truncate keeping k.  With
+ *                     cutoff > 0 the weight outside it is |theta - lo ro|^2;
+ *                     unless it exceeds the cutoff by more than its error
+ *                     (1e-12 + 2e-6 sqrt(weight), relative to |theta|^2) the
+ *                     call returns DMRG_ERR_PRECISION and the caller repeats
+ *                     the bond in FP64.  svals (may be NULL) receives the
+ *                     FP32-accurate Ritz values of the kept problem (digit
+ *                     Gram, FP32 Jacobi).
+ * keep receives the kept count (<= k); left_out is written as m x keep,
+ * right_out as keep x n (capacity m*k and k*n).  A basis that cannot be
+ * made orthonormal returns DMRG_ERR_NOCONV (callers fall back to
+ * dmrg_svd_truncate). */
+size_t dmrg_subspace_truncate_ex_workspace_bytes(int precision, int m, int n, int k);
+int dmrg_subspace_truncate_ex(int precision, int m, int n, int k, const void* theta, const void* start, int kstart,
+                              int absorb, int iters, double cutoff, int mindim, void* left_out, void* right_out,
+                              double* svals, int* keep, double* discarded, void* work, size_t work_bytes,
+                              void* stream);
+
+/* ---- symmetric eigendecomposition ----------------------------------------
+ * A (n x n, row-major, ld lda, symmetric) = V diag(w) V^T in FP64 by the
+ * parallel cyclic block-Jacobi method: 16-wide blocks, one CTA per block
+ * pair running a Jacobi sweep over the 32 x 32 subproblem in shared memory,
+ * the rotations applied to A and V as corrections by a second kernel per
+ * round; at most 40 sweeps.  w (host, n) receives the eigenvalues in
+ * descending order; V (device, n x n, ld ldv; may be NULL) the matching
+ * eigenvectors as columns.  Stands in for np.linalg.eigh in
+ * pyitensor/svd.py:131-133 and eigh_truncate (pyitensor/svd.py:71-88).
+ * DMRG_ERR_NOCONV if the last sweep still rotated.  Synchronises the
+ * stream. */
+size_t dmrg_syev_workspace_bytes(int n);
+int dmrg_syev(int n, const void* A, long long lda, double* w, void* V, long long ldv, int* sweeps, void* work,
+              size_t work_bytes, void* stream);
 
 /* ---- tile autotuner of the split-TF32 GEMM ------------------------------
  * The tensor-core GEMM uses 128 x 128 or 128 x 64 output tiles and walks
