@@ -749,9 +749,11 @@ int dmrg_subspace_truncate_ex(int precision, int m, int n, int k, const void* th
       const double rem = h[0] > 0.0 ? h[1] / h[0] : 0.0;
       // keep = k is the rule's answer when the weight beyond the kept space
       // exceeds the cutoff (no kept direction may then be dropped); decide it
-      // only when that holds beyond the estimate's own error, else leave
-      // the bond to the FP64 route
-      if (!(rem - (1e-12 + 2e-6 * std::sqrt(rem)) > cutoff)) return DMRG_ERR_PRECISION;
+      // only when that holds beyond the estimate's own error and beyond the
+      // few 1e-12 by which one product with the previous basis may miss the
+      // optimal subspace, else leave the bond to the FP64 route
+      if (!(rem - (1e-12 + 2e-6 * std::sqrt(rem)) > cutoff) || rem < 10.0 * cutoff + 1e-11)
+        return DMRG_ERR_PRECISION;
       disc = rem;
     }
     *keep = k;

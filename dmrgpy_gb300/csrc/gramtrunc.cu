@@ -493,10 +493,11 @@ int rr_truncate(int m, int n, int k, const double* theta, const double* X, int k
   DMRG_CUDA_TRY(cudaMemcpyAsync(&hacc, w.acc, sizeof(double), cudaMemcpyDeviceToHost, s));
   DMRG_CUDA_TRY(cudaStreamSynchronize(s));
   if (!(hacc == hacc)) return DMRG_ERR_NAN;
-  // Where the cutoff binds (fewer than k kept), the rule's forced drops are
-  // the weight beyond the subspace, so a subspace short of the optimal one
-  // by ~cutoff weight shifts the kept count along a flat spectrum; up to two
-  // more iterations (W = orth(Th^T U), then again) close that gap.
+  // Where the cutoff binds (fewer than k kept) or the weight beyond the
+  // subspace is within reach of it, the rule's forced drops are that weight,
+  // so a subspace short of the optimal one by ~cutoff weight shifts the kept
+  // count along a flat spectrum; up to two more iterations
+  // (W = orth(Th^T U), then again) close that gap.
   double* C = nullptr;
   std::vector<double> wt;
   int kp = 0;
@@ -535,7 +536,14 @@ int rr_truncate(int m, int n, int k, const double* theta, const double* X, int k
     DMRG_CUDA_TRY(cudaStreamSynchronize(s));
     double dc;
     keep_rule_partial(wt.data(), kw, std::min(m, n), hacc, cutoff, k, std::max(1, mindim), -1.0, &kp, &dc);
-    if (!(cutoff > 0.0 && kp < kw && round < 2)) break;
+    double kept_all = 0.0;
+    for (int j = 0; j < kw; ++j) kept_all += wt[j];
+    const double rem = hacc > 0.0 ? std::max(0.0, 1.0 - kept_all / hacc) : 0.0;
+    // one product with the previous basis leaves the subspace a few 1e-12
+    // (of the total weight) short of the optimal one: within that of the
+    // cutoff the rule's answer is not settled yet
+    const bool near = rem < 10.0 * cutoff + 1e-11;
+    if (!(cutoff > 0.0 && (kp < kw || near) && round < 2)) break;
     // W = orth(Th^T U), then the next round from it
     DMRG_TRY(gemm64(1, 0, N, kw, M, Th, N, res, k, w.Z, k, s));
     const int kz = kw;

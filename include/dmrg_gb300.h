@@ -254,17 +254,19 @@ int dmrg_subspace_truncate(int m, int n, int k, const void* theta, const void* s
  *                     largest Ritz value replaced by an orthonormal
  *                     completion), C = U^T theta; the rule runs on the
  *                     weights |C_j|^2 with the rest of |theta|^2 as forced
- *                     drops, and where it keeps fewer than k the subspace
- *                     gets up to two more iterations and the final count
- *                     comes from the Ritz values of theta theta^T on the
- *                     kept space.  svals (host, k) receives the
+ *                     drops; where it keeps fewer than k, or that weight is
+ *                     below 10 cutoff + 1e-11, the subspace gets up to two
+ *                     more iterations, and a count below k comes from the
+ *                     Ritz values of theta theta^T on the kept space.  svals (host, k) receives the
  *                     singular-value estimates.
  *   DMRG_PREC_TF32X3: the basis of dmrg_subspace_truncate keeping k.  With
  *                     cutoff > 0 the weight outside it is |theta - lo ro|^2;
  *                     unless it exceeds the cutoff by more than its error
- *                     (1e-12 + 2e-6 sqrt(weight), relative to |theta|^2) the
- *                     call returns DMRG_ERR_PRECISION and the caller repeats
- *                     the bond in FP64.  svals (may be NULL) receives the
+ *                     (1e-12 + 2e-6 sqrt(weight), relative to |theta|^2) and
+ *                     is above 10 cutoff + 1e-11 (the subspace may miss the
+ *                     optimal one by a few 1e-12) the call returns
+ *                     DMRG_ERR_PRECISION and the caller repeats the bond in
+ *                     FP64.  svals (may be NULL) receives the
  *                     FP32-accurate Ritz values of the kept problem (digit
  *                     Gram, FP32 Jacobi).
  * keep receives the kept count (<= k); left_out is written as m x keep,

