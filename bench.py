@@ -15,10 +15,16 @@ JSON line keys beyond the common contract:
                CUDA events on the launching stream;
   cpu_baseline the CPU oracle (NumPy restatement of the reference sweep)
                on the host cores, one bond at chi=1024;
-  sweep        per-phase seconds, Lanczos iterations, refined energy.
+  sweep        per-phase seconds, Lanczos iterations, refined energy and
+               the end-spin correlator <S^z_1 S^z_N>;
+  fp64_gpu     one measured FP64 GPU sweep at chi=1024 from the split-TF32
+               state: seconds, refined energy, |dE|/N and the correlator
+               difference against the split-TF32 state;
+  e2e          one sweep through dmrgpy_gb300.Chain with the MPS in host
+               memory before and after.
 
---impl reference runs the oracle on the host cores instead (one bond of the
-same workload per step).
+--impl reference runs the oracle on the host cores instead (one bond update
+of the same workload per step).
 """
 import argparse
 import json
@@ -121,28 +127,6 @@ def profile_summary():
 
 
 # ---------------------------------------------------------------- CPU oracle sample
-def cpu_bond_sample(L, Wi, Wj, R, theta, Lnext_A, k_lanczos, maxdim):
-    """One C2 bond at chi=1024 on the host with the oracle (complex128, as
-    the reference computes): one H_eff matvec, one truncated SVD, one
-    environment extension; the bond time is k_lanczos matvecs + SVD + env."""
-    import numpy as np
-    import oracle as O
-    Lc, Wic, Wjc, Rc, thc = (np.asarray(x, dtype=np.complex128) for x in (L, Wi, Wj, R, theta))
-    t0 = time.perf_counter()
-    O.heff2_matvec(Lc, Wic, Wjc, Rc, thc)
-    t_mv = time.perf_counter() - t0
-    cl, d1, d2, cr = thc.shape
-    t0 = time.perf_counter()
-    O.svd_truncated(thc.reshape(cl * d1, d2 * cr), 0.0, maxdim, 1)
-    t_svd = time.perf_counter() - t0
-    A = np.asarray(Lnext_A, dtype=np.complex128)
-    t0 = time.perf_counter()
-    O.extend_left(Lc, Wic, A)
-    t_env = time.perf_counter() - t0
-    t_bond = k_lanczos * t_mv + t_svd + t_env
-    return {"t_matvec": t_mv, "t_svd": t_svd, "t_env": t_env, "t_bond": t_bond}
-
-
 def max_over_ranks(value, dist, device):
     """The largest of the ranks' values (the job's time is that of its
     slowest replica); the value itself in a single process."""
@@ -172,42 +156,76 @@ def host_cores():
         return os.cpu_count()
 
 
-def run_reference(args):
-    """--impl reference: the oracle port on the host cores, one C2 bond at
-    chi=1024 per step (random environments of the right shapes)."""
+def reference_bond_step(L, Wi, Wj, R, theta, A, k, maxdim):
+    """One chi=1024 bond update of the reference algorithm on the host with
+    the oracle (NumPy complex128, as the reference computes): k H_eff
+    matvecs (each one run and timed, the Krylov count of the GPU sweep),
+    the truncated SVD and one environment extension; the wall time of the
+    whole step is measured."""
     import numpy as np
-    from dmrgpy_gb300 import mpo as M
+    import oracle as O
+    t0 = time.perf_counter()
+    x = theta
+    t_mv = []
+    for _ in range(k):
+        a = time.perf_counter()
+        y = O.heff2_matvec(L, Wi, Wj, R, x)
+        t_mv.append(time.perf_counter() - a)
+        x = y / np.linalg.norm(y)
+    cl, d1, d2, cr = theta.shape
+    a = time.perf_counter()
+    O.svd_truncated(x.reshape(cl * d1, d2 * cr), 0.0, maxdim, 1)
+    t_svd = time.perf_counter() - a
+    a = time.perf_counter()
+    O.extend_left(L, Wi, A)
+    t_env = time.perf_counter() - a
+    return {"t_matvecs": t_mv, "t_svd": t_svd, "t_env": t_env, "t_step": time.perf_counter() - t0}
+
+
+def run_reference(args):
+    """--impl reference: the oracle restatement of the reference sweep on
+    the host cores.  A step is one bond update of the headline workload at
+    chi=1024 (S=1 Heisenberg, d=3, the MPO from the oracle's own builder,
+    seeded random environments and two-site tensor of the chi=1024 shapes):
+    3 matvecs (the mean Lanczos count of the GPU sweep at this bond size),
+    the truncated SVD and an environment extension, timed as one wall-clock
+    step.  A full sweep is 198 such steps."""
+    import numpy as np
+    import oracle as O
     from dmrgpy_gb300.engine import Engine
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    W, _ = M.build_mpo([3] * 6, terms_heisenberg(6))
+    W = O.build_mpo([3] * 6, terms_heisenberg(6))
     Wi, Wj = W[2], W[3]
     rng = np.random.default_rng(0)
     w = Wi.shape[0]
-    L = rng.standard_normal((CHI, w, CHI))
-    R = rng.standard_normal((CHI, w, CHI))
-    th = rng.standard_normal((CHI, D, D, CHI))
-    A = rng.standard_normal((CHI, D, CHI))
-    k = 10
-    flops = Engine.heff2_flops(CHI, D, D, CHI, w, w, w)
+    c = np.complex128
+    L = rng.standard_normal((CHI, w, CHI)).astype(c)
+    R = rng.standard_normal((CHI, w, CHI)).astype(c)
+    th = rng.standard_normal((CHI, D, D, CHI)).astype(c)
+    A = rng.standard_normal((CHI, D, CHI)).astype(c)
+    k = 3
+    flops = Engine.heff2_flops(CHI, D, D, CHI, w, Wi.shape[3], Wj.shape[3], complex_=False)
     for _ in range(args.warmup):
-        cpu_bond_sample(L, Wi, Wj, R, th, A, 1, CHI)
+        reference_bond_step(L, Wi, Wj, R, th, A, 1, CHI)
     tot, res = 0.0, None
     for _ in range(args.steps):
-        res = cpu_bond_sample(L, Wi, Wj, R, th, A, k, CHI)
-        tot += res["t_bond"]
+        res = reference_bond_step(L, Wi, Wj, R, th, A, k, CHI)
+        tot += res["t_step"]
     value = k * flops * args.steps / tot / 1e12
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic", "config": {"workload": "S=1 Heisenberg N=100 d=3 w=5 chi=1024 bond update",
-                                            "parallelism": "host"},
+            "data": "synthetic: seeded random chi=1024 environments and two-site tensor",
+            "config": {"workload": "S=1 Heisenberg N=100 d=3 w=5 chi=1024: one bond update per step "
+                                   "(198 per sweep)", "parallelism": "host"},
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port",
-                             "sample": "one chi=1024 bond: %d matvecs (timed once) + truncated SVD + env; oracle "
-                                       "NumPy complex128" % k},
+                             "sample": "one chi=1024 bond update of the oracle (NumPy complex128 like the "
+                                       "reference): %d matvecs, each run, + truncated SVD + environment "
+                                       "extension, wall time per step" % k},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "components_s": res}
+            "components_s": res, "sweep_s_equivalent": 198 * tot / args.steps}
     print(json.dumps(line))
     return 0
 
@@ -235,12 +253,14 @@ def run_gpu(args):
     np.random.seed(1234 + rank)
     A = eng.to_device(MP.random_arrays([D] * N_SITES, 64))
     eng.canonicalize_right_to_left_of(A)
-    # ramp (not timed): chi 64 -> 256
+    # ramp (not timed): chi 64 -> 256, then the warm-up steps at chi=1024
+    t_ramp = time.perf_counter()
     for chi in (64, 256):
         eng.sweep(A, chi, 0.0, 2)
-    # warm-up steps at chi=1024
     for _ in range(args.warmup):
         eng.sweep(A, CHI, 0.0, 2)
+    torch.cuda.synchronize()
+    t_ramp = time.perf_counter() - t_ramp
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -314,62 +334,71 @@ def run_gpu(args):
             "tf32x3_ceiling_tflops": bf16 / 2.0 / 3.0,
             "frac_of_tf32x3_ceiling": achieved / (bf16 / 2.0 / 3.0)}
 
-    # --- the FP64 GPU path on the same chi=1024 bond (the metric's comparison):
-    # one FP64 bond update = mean-iterations FP64 matvecs + FP64 Jacobi
-    # truncation + FP64 environment extension, each timed with CUDA events;
-    # a full FP64 sweep is that bond time x the bond updates of a sweep
-    fp64 = None
-    if not args.no_fp64:
-        e64 = Engine(W, real=real, precision="fp64", device="cuda:%d" % local)
-        h64 = e64.heff2(lenv[mid - 1], e64.W[mid - 1], e64.W[mid], renv[mid + 2], theta.shape)
-
-        def timed(fn, reps=1):
-            fn()
-            torch.cuda.synchronize()
-            a0 = torch.cuda.Event(enable_timing=True)
-            a1 = torch.cuda.Event(enable_timing=True)
-            a0.record()
-            for _ in range(reps):
-                fn()
-            a1.record()
-            torch.cuda.synchronize()
-            return a0.elapsed_time(a1) / 1e3 / reps
-
-        t64_mv = timed(lambda: e64.apply(h64, theta), 2)
-        m2 = cl * d1
-        t64_svd = timed(lambda: e64.svd(theta.view(m2, -1), 0.0, CHI, 1, 0))
-        t64_env = timed(lambda: e64.env_left(lenv[mid - 1], e64.W[mid - 1], A[mid - 1], fp64=True))
-        k_mean = float(np.mean(iters)) if iters else 3.0
-        bond64 = k_mean * t64_mv + t64_svd + t64_env
-        nb = len(st.records) / max(1, args.steps)
-        fp64 = {"matvec_s": t64_mv, "svd_s": t64_svd, "env_s": t64_env, "bond_s": bond64,
-                "sweep_s_est": bond64 * nb, "speedup_vs_fp64_est": bond64 * nb / (elapsed / args.steps),
-                "note": "FP64 GPU bond update at the chi=1024 middle bond (same state), times the %d bond "
-                        "updates of a sweep; matvec count = mean Lanczos iterations of the split-TF32 sweep" % nb}
-        del e64, h64
-
-    # --- FP64 refinement of the energy of the final state (not in the timed steps)
+    # --- FP64 refinement of the energy of the split-TF32 state (not in the
+    # timed steps) and the end-spin correlator, both on the device
     t0 = time.perf_counter()
     e_ref = eng.energy_fp64(A)
     t_refine = time.perf_counter() - t0
+    Wc, _ = M.build_mpo([3] * N_SITES, [(1.0 + 0j, [("Sz", 1), ("Sz", N_SITES)])])
+    corr_eng = Engine(Wc, real=True, precision="fp64", device="cuda:%d" % local)
+    szsz32 = corr_eng.energy_fp64(A)
 
-    # --- end-to-end through the public session API: host MPS in, sweep, host MPS out
+    # --- the FP64 GPU path (the metric's comparison), measured: one full FP64
+    # sweep at chi=1024 continuing from the split-TF32 state (right
+    # environments rebuilt in FP64 first, not timed), its refined energy and
+    # correlator; |dE|/N compares the two refined energies
+    fp64 = None
+    if not args.no_fp64:
+        e64 = Engine(W, real=real, precision="fp64", device="cuda:%d" % local)
+        A64 = [a.clone() for a in A]
+        e64._renv = e64.right_envs(A64)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        f0.record()
+        e64_last = e64.sweep(A64, CHI, 0.0, 2, record=True)
+        f1.record()
+        torch.cuda.synchronize()
+        t64 = f0.elapsed_time(f1) / 1e3
+        w64 = time.perf_counter() - w0
+        e64_ref = e64.energy_fp64(A64)
+        szsz64 = corr_eng.energy_fp64(A64)
+        it64 = [r["iters"] for r in e64.stats.records]
+        fp64 = {"sweep_s": t64, "wall_s": w64, "phase_s": dict(e64.stats.t),
+                "matvecs": e64.stats.matvecs, "lanczos_iters_mean": float(np.mean(it64)) if it64 else None,
+                "energy_last_bond": e64_last, "energy_refined": e64_ref,
+                "abs_dE_per_site": abs(e_ref - e64_ref) / N_SITES,
+                "szsz_1N": szsz64, "abs_d_szsz_1N": abs(szsz32 - szsz64),
+                "speedup_sweep": t64 / (elapsed / args.steps),
+                "note": "one measured FP64 GPU sweep at chi=1024 (FP64 matvecs, FP64 subspace + Rayleigh-Ritz "
+                        "truncation, FP64 environments) from the split-TF32 state; |dE|/N = |E_refined(split-TF32 "
+                        "state) - E_refined(FP64-swept state)| / N"}
+        del e64, A64
+
+    # --- end-to-end through the public session API (dmrgpy_gb300.Chain, the
+    # object dmrgpy's glue drives): the MPS handed over from host memory,
+    # the MPO compiled, one split-TF32 sweep at chi=1024, the MPS back on
+    # the host
+    from dmrgpy_gb300 import Chain
     host = eng.to_host(A)
     h2d = sum(a.nbytes for a in host)
-    pinned = [torch.from_numpy(a).pin_memory() for a in host]
-    eng.invalidate()
-    eng.stats = SweepStats()
+    chain = Chain([3] * N_SITES, precision="tf32x3")
+    chain.set_sweep_params(CHI, 1, 0.0, 0.0)
+    chain.set_hamiltonian(terms_heisenberg(N_SITES))
+    chain.set_wavefunction(MP.MPS(host, center=1))
+    del host
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    Ad = [p.to(eng.device, non_blocking=True) for p in pinned]
-    eng.sweep(Ad, CHI, 0.0, 2)
-    out = [a.to("cpu") for a in Ad]
+    e_chain = chain.gs_energy()
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
-    d2h = sum(o.numel() * o.element_size() for o in out)
-    e2e = {"value": eng.stats.matvec_flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "sweep_s": t_e2e,
-           "note": "MPS copied host->device, right environments rebuilt, one sweep, MPS copied back"}
+    d2h = sum(a.nbytes for a in chain.gs_wavefunction().tensors)
+    e2e = {"value": chain.last_stats.matvec_flops / t_e2e / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "sweep_s": t_e2e, "energy_last_bond": e_chain,
+           "note": "Chain(precision='tf32x3'): set_wavefunction(host MPS) + gs_energy() with one sweep at "
+                   "chi=1024: MPO compile, MPS host->device, right environments, the sweep, MPS device->host"}
+    del chain
 
     line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -386,20 +415,24 @@ def run_gpu(args):
                       "lanczos_iters_mean": float(np.mean(iters)) if iters else None,
                       "chi_max": max(chis) if chis else None,
                       "energy_last_bond_tf32": energy, "energy_refined_fp64": e_ref,
-                      "energy_per_site": e_ref / N_SITES, "refine_s": t_refine}}
+                      "energy_per_site": e_ref / N_SITES, "refine_s": t_refine, "szsz_1N": szsz32,
+                      "schedule_s_before_timed": t_ramp}}
     if rank == 0 and not args.no_cpu:
         k_mean = int(round(np.mean(iters))) if iters else 10
         Lh = lenv[mid - 1].cpu().numpy()
         Rh = renv[mid + 2].cpu().numpy()
         thh = theta.cpu().numpy()
         Ah = A[mid - 1].cpu().numpy()
-        res = cpu_bond_sample(Lh, W[mid - 1], W[mid], Rh, thh, Ah, k_mean, CHI)
-        cpu_val = k_mean * f_mv / res["t_bond"] / 1e12
+        c = np.complex128
+        res = reference_bond_step(Lh.astype(c), W[mid - 1].astype(c), W[mid].astype(c), Rh.astype(c),
+                                  thh.astype(c), Ah.astype(c), k_mean, CHI)
+        cpu_val = k_mean * f_mv / res["t_step"] / 1e12
         line["cpu_baseline"] = {"value": cpu_val, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port",
-                                "sample": "one chi=1024 bond of this workload on the host: oracle NumPy "
-                                          "(complex128 like the reference) matvec x %d (mean Lanczos "
-                                          "iterations of the GPU sweep) + truncated SVD + env extension" % k_mean,
-                                "components_s": res}
+                                "sample": "one chi=1024 bond update of this state on the host: oracle NumPy "
+                                          "(complex128 like the reference), %d matvecs (the mean Lanczos count "
+                                          "of the GPU sweep), each run, + truncated SVD + env extension, wall "
+                                          "time" % k_mean,
+                                "components_s": res, "sweep_s_equivalent": 198 * res["t_step"]}
     if rank == 0:
         print(json.dumps(line))
     if dist:
@@ -414,7 +447,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
-    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU bond sample")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the measured FP64 GPU sweep")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -12,8 +12,9 @@ names).
 Differences, all numerical-path only: the MPO is compiled by the automaton
 builder of :mod:`dmrgpy_gb300.mpo` (real arithmetic whenever the Hamiltonian
 allows); the right environments of a sweep are reused from the previous
-right-to-left pass instead of being rebuilt; truncations use the one-sided
-Jacobi SVD.
+right-to-left pass instead of being rebuilt; truncations take the
+reference's Gram-matrix route on the GPU (blocked-Jacobi eigensolver) or,
+on large bonds where maxdim binds, a subspace + Rayleigh-Ritz form of it.
 """
 import numpy as np
 

@@ -271,13 +271,21 @@ class Engine:
         kp = keep.value
         return lo[:m * kp].view(m, kp), ro[:kp * n].view(kp, n), s, kp, disc.value
 
-    def use_subspace(self, m, n, cutoff, maxdim):
-        """Real sweeps whose truncation is bound by maxdim on a large bond use
-        the subspace route (split-TF32 or FP64 products by the engine's
-        precision)."""
+    def use_subspace(self, m, n, cutoff, maxdim, absorb=0):
+        """Real sweeps on a large bond use the subspace route (split-TF32 or
+        FP64 products by the engine's precision) where maxdim binds, and
+        where the full rank min(m, n) is kept but the kept side is more than
+        twice that (a Gram matrix of the kept side would be oversized; with
+        the other side's tensor as the start the subspace is then exact)."""
         if not (self.real and maxdim and maxdim > 0):
             return False
-        return min(m, n) >= SUBSPACE_MIN_DIM and maxdim < min(m, n)
+        c = min(m, n)
+        if c < SUBSPACE_MIN_DIM:
+            return False
+        if maxdim < c:
+            return True
+        kept = m if absorb == 0 else n
+        return kept > 2 * c
 
     def use_identity_split(self, m, n, cutoff, maxdim, absorb):
         """Split-TF32 sweeps that keep the whole kept side with no cutoff:
@@ -459,7 +467,7 @@ class Engine:
             tm = theta.view(m, n)
             lo, ro = (eye, tm) if absorb == 0 else (tm, eye)
             s, keep, disc = None, rank, 0.0
-        elif self.use_subspace(m, n, cutoff, maxdim):
+        elif self.use_subspace(m, n, cutoff, maxdim, absorb):
             # warm start: the orthonormal tensor on the other side of the bond
             # (right-canonical A_j in a left-to-right pass, left-canonical A_i
             # in a right-to-left pass)
