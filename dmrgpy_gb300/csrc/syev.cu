@@ -64,6 +64,7 @@ struct SyevWs {
   int np, nb, npair;
   double* G;                 // np x np (FP32 runs use the first half)
   double* V;                 // np x np
+  double* T;                 // np x np (FP64 runs with an FP32 presolve)
   double* R;                 // npair x 32 x 32: D = R - I of each pair
   int* ident;                // npair
   int* pairs;                // (nb-1) x npair x 2
@@ -87,6 +88,7 @@ size_t syev_layout(int n, SyevWs* w, void* base) {
   s.np = np; s.nb = nb; s.npair = npair;
   s.G = static_cast<double*>(take(sizeof(double) * (size_t)np * np));
   s.V = static_cast<double*>(take(sizeof(double) * (size_t)np * np));
+  s.T = static_cast<double*>(take(sizeof(double) * (size_t)np * np));
   s.R = static_cast<double*>(take(sizeof(double) * (size_t)npair * JP * JP));
   s.ident = static_cast<int*>(take(sizeof(int) * npair));
   s.pairs = static_cast<int*>(take(sizeof(int) * 2 * (size_t)(nb - 1 > 0 ? nb - 1 : 1) * npair));
@@ -322,6 +324,35 @@ __global__ void __launch_bounds__(256) syev_apply_kernel(T* __restrict__ G, T* _
     V[(long long)(rt * JP + i) * np + pair_index(xb0, xb1, j0 + q)] = x[i][j0 + q] + o[q];
 }
 
+// out (double, np x np) = in (float, np x np)
+__global__ void syev_widen_kernel(const float* __restrict__ in, double* __restrict__ out, long long total) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x)
+    out[e] = (double)in[e];
+}
+
+// B = 1.5 I - 0.5 B in place (the Newton-Schulz factor from B = Q^T Q)
+__global__ void syev_ns_kernel(double* __restrict__ B, int np) {
+  const long long total = (long long)np * np;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / np), j = (int)(e - (long long)i * np);
+    B[e] = (i == j ? 1.5 : 0.0) - 0.5 * B[e];
+  }
+}
+
+// *scale = max_i |G_ii| as ordered bits
+__global__ void syev_scale_kernel(const double* __restrict__ G, int np, unsigned long long* __restrict__ scale) {
+  unsigned long long mx = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    const double a = fabs(G[(long long)i * np + i]);
+    unsigned long long b;
+    memcpy(&b, &a, sizeof(b));
+    if (a == a && b > mx) mx = b;
+  }
+  if (mx) atomicMax(scale, mx);
+}
+
 template <typename T>
 __global__ void syev_diag_kernel(const T* __restrict__ G, int np, double* __restrict__ d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -364,24 +395,14 @@ void tournament(int nb, std::vector<int>& out) {
     }
 }
 
+// sweeps over (G, V) until one rotates nothing (at most max_sweeps)
 template <typename T>
-int syev_impl(int n, const double* A, long long lda, double* w, int max_sweeps, int* sweeps, void* work,
-              cudaStream_t s) {
-  SyevWs ws;
-  syev_layout(n, &ws, work);
-  const int np = ws.np, nb = ws.nb, npair = ws.npair, rounds = nb - 1;
-  T* G = reinterpret_cast<T*>(ws.G);
-  T* V = reinterpret_cast<T*>(ws.V);
+int syev_sweeps(SyevWs& ws, T* G, T* V, int max_sweeps, int* done, int* converged, cudaStream_t s) {
+  const int np = ws.np, npair = ws.npair, rounds = ws.nb - 1;
   T* R = reinterpret_cast<T*>(ws.R);
-  std::vector<int> tab;
-  tournament(nb, tab);
-  DMRG_CUDA_TRY(cudaMemcpyAsync(ws.pairs, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, s));
-  DMRG_CUDA_TRY(cudaMemsetAsync(ws.scale, 0, sizeof(unsigned long long), s));
-  syev_init_kernel<T><<<grid_for((long long)np * np), 256, 0, s>>>(A, lda, n, np, G, V, ws.scale);
-  DMRG_CHECK_LAUNCH();
   const int apply_grid = npair * npair + (np / JP) * npair;
-  int sw = 0, converged = 0;
-  for (; sw < max_sweeps && !converged; ++sw) {
+  int sw = 0, conv = 0;
+  for (; sw < max_sweeps && !conv; ++sw) {
     DMRG_CUDA_TRY(cudaMemsetAsync(ws.flag, 0, sizeof(int), s));
     for (int r = 0; r < rounds; ++r) {
       const int* pr = ws.pairs + (size_t)2 * r * npair;
@@ -393,9 +414,27 @@ int syev_impl(int n, const double* A, long long lda, double* w, int max_sweeps, 
     int h = 0;
     DMRG_CUDA_TRY(cudaMemcpyAsync(&h, ws.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     DMRG_CUDA_TRY(cudaStreamSynchronize(s));
-    converged = h == 0;
+    conv = h == 0;
   }
-  if (sweeps) *sweeps = sw;
+  *done += sw;
+  *converged = conv;
+  return DMRG_OK;
+}
+
+// C (np x np) = A B, all np x np row-major FP64
+int syev_gemm(int np, const double* A, const double* B, double* C, cudaStream_t s) {
+  TGemm g{};
+  g.B = ax(1); g.M = ax(np); g.K = ax(np); g.N = ax(np);
+  g.a_m = st(np); g.a_k = st(1);
+  g.b_k = st(np); g.b_n = st(1);
+  g.c_m = st(np); g.c_n = st(1);
+  return tgemm<double>(g, 1.0, A, B, 0.0, C, s);
+}
+
+// Sorted eigenvalues to the host and the permutation to the workspace.
+template <typename T>
+int syev_finish(int n, SyevWs& ws, const T* G, double* w, cudaStream_t s) {
+  const int np = ws.np;
   syev_diag_kernel<T><<<(np + 255) / 256, 256, 0, s>>>(G, np, ws.diag);
   DMRG_CHECK_LAUNCH();
   std::vector<double> d(n);
@@ -410,7 +449,83 @@ int syev_impl(int n, const double* A, long long lda, double* w, int max_sweeps, 
   DMRG_CUDA_TRY(cudaMemcpyAsync(ws.perm, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   // the host vector perm must outlive the copy
   DMRG_CUDA_TRY(cudaStreamSynchronize(s));
-  return converged ? DMRG_OK : DMRG_ERR_NOCONV;
+  return DMRG_OK;
+}
+
+// Eigenvectors of an FP64 matrix from n = 256 on come from an FP32 presolve
+// and an FP64 polish: the FP32 sweeps (64x the FP64 rate on GB300) take the
+// matrix from cold to off-diagonals ~1e-6 of the diagonal; their rotation Q
+// is made orthonormal in FP64 by two Newton-Schulz steps
+// (Q <- Q (3 I - Q^T Q) / 2), the matrix transformed as Q^T A Q in FP64, and
+// the FP64 sweeps, starting from V = Q, converge quadratically from there
+// (two or three sweeps instead of the ten to fifteen of a cold start).
+constexpr int PRESOLVE_MIN_N = 256;
+
+template <typename T>
+int syev_impl(int n, const double* A, long long lda, double* w, int max_sweeps, int* sweeps, void* work,
+              cudaStream_t s) {
+  SyevWs ws;
+  syev_layout(n, &ws, work);
+  const int np = ws.np, nb = ws.nb;
+  std::vector<int> tab;
+  tournament(nb, tab);
+  DMRG_CUDA_TRY(cudaMemcpyAsync(ws.pairs, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, s));
+  DMRG_CUDA_TRY(cudaMemsetAsync(ws.scale, 0, sizeof(unsigned long long), s));
+  int done = 0, conv = 0;
+  const bool presolve = sizeof(T) == 8 && n >= PRESOLVE_MIN_N;
+  if (!presolve) {
+    T* G = reinterpret_cast<T*>(ws.G);
+    T* V = reinterpret_cast<T*>(ws.V);
+    syev_init_kernel<T><<<grid_for((long long)np * np), 256, 0, s>>>(A, lda, n, np, G, V, ws.scale);
+    DMRG_CHECK_LAUNCH();
+    DMRG_TRY(syev_sweeps<T>(ws, G, V, max_sweeps, &done, &conv, s));
+    if (sweeps) *sweeps = done;
+    DMRG_TRY(syev_finish<T>(n, ws, G, w, s));
+    return conv ? DMRG_OK : DMRG_ERR_NOCONV;
+  }
+  // FP32 presolve: G32 in ws.G, V32 in ws.T
+  float* G32 = reinterpret_cast<float*>(ws.G);
+  float* V32 = reinterpret_cast<float*>(ws.T);
+  syev_init_kernel<float><<<grid_for((long long)np * np), 256, 0, s>>>(A, lda, n, np, G32, V32, ws.scale);
+  DMRG_CHECK_LAUNCH();
+  int done32 = 0;
+  DMRG_TRY(syev_sweeps<float>(ws, G32, V32, 15, &done32, &conv, s));
+  const long long nn = (long long)np * np;
+  syev_widen_kernel<<<grid_for(nn), 256, 0, s>>>(V32, ws.V, nn);    // Q0 (ws.V)
+  DMRG_CHECK_LAUNCH();
+  // two Newton-Schulz steps: ws.V -> ws.T -> ws.V
+  double* src = ws.V;
+  double* dst = ws.T;
+  for (int it = 0; it < 2; ++it) {
+    DMRG_TRY(tgemm_gram(src, np, np, np, ws.G, s));                  // B = Q^T Q
+    syev_ns_kernel<<<grid_for(nn), 256, 0, s>>>(ws.G, np);            // B = 1.5 I - 0.5 B
+    DMRG_CHECK_LAUNCH();
+    DMRG_TRY(syev_gemm(np, src, ws.G, dst, s));                      // Q B
+    std::swap(src, dst);
+  }
+  // G = Q^T A Q (the padded rows and columns of A are zero): P = A Q[:n] in
+  // ws.T, then Q^T P in ws.G
+  {
+    TGemm g{};
+    g.B = ax(1); g.M = ax(n); g.K = ax(n); g.N = ax(np);
+    g.a_m = st(lda); g.a_k = st(1);
+    g.b_k = st(np); g.b_n = st(1);
+    g.c_m = st(np); g.c_n = st(1);
+    DMRG_TRY(tgemm<double>(g, 1.0, A, ws.V, 0.0, ws.T, s));
+    TGemm h{};
+    h.B = ax(1); h.M = ax(np); h.K = ax(n); h.N = ax(np);
+    h.a_m = st(1); h.a_k = st(np);
+    h.b_k = st(np); h.b_n = st(1);
+    h.c_m = st(np); h.c_n = st(1);
+    DMRG_TRY(tgemm<double>(h, 1.0, ws.V, ws.T, 0.0, ws.G, s));
+  }
+  DMRG_CUDA_TRY(cudaMemsetAsync(ws.scale, 0, sizeof(unsigned long long), s));
+  syev_scale_kernel<<<(np + 255) / 256, 256, 0, s>>>(ws.G, np, ws.scale);
+  DMRG_CHECK_LAUNCH();
+  DMRG_TRY(syev_sweeps<double>(ws, ws.G, ws.V, max_sweeps, &done, &conv, s));
+  if (sweeps) *sweeps = done;
+  DMRG_TRY(syev_finish<double>(n, ws, ws.G, w, s));
+  return conv ? DMRG_OK : DMRG_ERR_NOCONV;
 }
 
 }  // namespace

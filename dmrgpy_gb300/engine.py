@@ -276,10 +276,14 @@ class Engine:
         FP64 products by the engine's precision) where maxdim binds, and
         where the full rank min(m, n) is kept but the kept side is more than
         twice that (a Gram matrix of the kept side would be oversized; with
-        the other side's tensor as the start the subspace is then exact)."""
+        the other side's tensor as the start the subspace is then exact);
+        split-TF32 sweeps without a cutoff take it for every full-rank bond."""
         if not (self.real and maxdim and maxdim > 0):
             return False
         c = min(m, n)
+        if self.prec == _lib.PREC_TF32X3 and cutoff <= 0.0 and maxdim >= c:
+            # the full rank is kept: the subspace is exact at any size
+            return True
         if c < SUBSPACE_MIN_DIM:
             return False
         if maxdim < c:
