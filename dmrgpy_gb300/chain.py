@@ -150,30 +150,45 @@ class Chain:
         self._wf0_energy = None
 
     # ---------------------------------------------------------------- measurements
-    def _norm_tensors(self, wf):
-        nrm = _mps.inner(wf.tensors, wf.tensors).real ** 0.5
-        t = [a.copy() for a in wf.tensors]
-        t[0] = t[0] / nrm
-        return t
+    # Contracted on the device in FP64 (Engine.transition / bond_spectrum);
+    # the state crosses to the device once per call.
+    def _measure_engine(self, W, real, wfs):
+        real = real and not any(np.iscomplexobj(t) for wf in wfs for t in wf.tensors)
+        return Engine(W, real=real, precision="fp64")
 
     def vev(self, terms, wf, npow=1):
-        if npow != 1:
-            raise NotImplementedError("vev with npow > 1 is not provided by the GB300 backend")
+        """pyitensor/chain.py:277-287: <psi|A^npow|psi>/<psi|psi>; A^npow is
+        formed exactly as an MPO power (bond dimension w^npow) rather than
+        by npow-1 truncated applications."""
         op = self.build_operator(terms)
-        t = self._norm_tensors(wf)
-        return _mps.expect(t, op.W, t)
+        W = _mpo_power(op.W, int(npow))
+        eng = self._measure_engine(W, op.real, [wf])
+        A = eng.to_device(wf.tensors)
+        num = eng.transition(eng.W, A, A)
+        den = eng.transition(eng.identity_mpo(self.dims), A, A)
+        return num / den.real
 
     def overlap(self, wf1, wf2):
-        return _mps.inner(wf1.tensors, wf2.tensors)
+        eng = self._measure_engine([np.eye(d).reshape(1, d, d, 1) for d in self.dims], True, [wf1, wf2])
+        return eng.transition(eng.W, eng.to_device(wf1.tensors), eng.to_device(wf2.tensors))
 
     def overlap_aMb(self, wf1, terms, wf2):
-        return _mps.expect(wf1.tensors, self.build_operator(terms).W, wf2.tensors)
+        op = self.build_operator(terms)
+        return self.overlap_aMb_operator(wf1, op, wf2)
 
     def overlap_aMb_operator(self, wf1, A, wf2):
-        return _mps.expect(wf1.tensors, A.W, wf2.tensors)
+        eng = self._measure_engine(A.W, A.real, [wf1, wf2])
+        return eng.transition(eng.W, eng.to_device(wf1.tensors), eng.to_device(wf2.tensors))
 
     def bond_entropy(self, wf, b):
-        return _mps.bond_entropy(wf.tensors, b)
+        """pyitensor/chain.py:468-480: -sum p log p over the Schmidt weights
+        p > 1e-12 across bond (b, b+1)."""
+        eng = self._measure_engine([np.eye(d).reshape(1, d, d, 1) for d in self.dims], True, [wf])
+        s = eng.bond_spectrum(eng.to_device(wf.tensors), int(b))
+        p = s ** 2
+        p = p / p.sum()
+        p = p[p > 1e-12]
+        return float(-np.sum(p * np.log(p)))
 
     # ---------------------------------------------------------------- time evolution
     def tdvp_step(self, H, wf, dt, num_center=2):
@@ -220,6 +235,24 @@ class Chain:
             nrm = _torch_norm(A)
             A[0] = A[0] * (norm0 / nrm)
         return out, _mps.MPS(eng.to_host(A), center=1)
+
+
+def _mpo_power(W, k):
+    """The MPO of A^k (k >= 1) for A given as (w_l, d_in, d_out, w_r) site
+    tensors, without truncation: per site the product of k copies, bond
+    dimension w^k."""
+    if k < 1:
+        raise ValueError("npow must be >= 1")
+    out = [np.asarray(w) for w in W]
+    for _ in range(k - 1):
+        nxt = []
+        for p, w in zip(out, W):
+            # apply w after p: (pl, wl, din, dout, pr, wr)
+            x = np.einsum("aimb,cmoe->acio be".replace(" ", ""), p, np.asarray(w))
+            pl, wl, d, _, pr, wr = x.shape
+            nxt.append(x.reshape(pl * wl, d, d, pr * wr))
+        out = nxt
+    return out
 
 
 def _torch_norm(A):

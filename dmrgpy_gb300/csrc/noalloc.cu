@@ -11,8 +11,12 @@
 //
 // Rules of use:
 //   * The first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current) and caches it; make
-//     that first call before any stream capture.
+//     cudaGetSymbolAddress (with that device current) and caches it by
+//     device number; make that first call before any stream capture.  The
+//     cache assumes the device's primary context (the runtime's) and no
+//     cudaDeviceReset between calls, after which the address would be stale.
+//   * The array belongs to the library's device image, so every device that
+//     loads the library holds its 64 MiB until exit, called or not.
 //   * Every call on every stream shares the one array: two calls whose
 //     executions overlap (different streams, or host threads without
 //     ordering between them) overwrite each other's intermediates and give

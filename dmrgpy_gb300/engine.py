@@ -380,6 +380,46 @@ class Engine:
             L = self.env_mixed(0, L, W, B, A)
         return complex(L.reshape(-1)[0].item()), grads
 
+    # ------------------------------------------------------------ measurements
+    def transition(self, W, bra, ket):
+        """<bra|W|ket> on the device in FP64 (pyitensor/mpsalgebra.py:66-106,
+        inner with an MPO): the left transition environment carried across
+        the chain.  W: device MPO tensors of the engine's dtype (self.W for
+        the engine's own operator); bra, ket: device site tensors."""
+        L = self.edge
+        for w, b, a in zip(W, bra, ket):
+            L = self.env_mixed(0, L, w, b, a)
+        return complex(L.reshape(-1)[0].item())
+
+    def identity_mpo(self, dims):
+        torch = _torch()
+        return [torch.eye(d, dtype=self.tdtype, device=self.device).reshape(1, d, d, 1).contiguous() for d in dims]
+
+    def bond_spectrum(self, A, b):
+        """Schmidt values across bond (b, b+1), 1-based, of the device MPS A
+        (descending, host array): a copy is brought into mixed canonical
+        form by lossless device factorisations from both ends and the
+        two-site tensor across the bond factorised (the measurement of
+        pyitensor/chain.py:468-480)."""
+        A = [a.clone() for a in A]
+        n = len(A)
+        for i in range(b - 1):
+            cl, d, cr = A[i].shape
+            lo, ro, _, k, _ = self.svd(A[i].reshape(cl * d, cr), -1.0, 0, 1, 0)
+            A[i] = lo.reshape(cl, d, k)
+            nxt = A[i + 1]
+            A[i + 1] = self.gemm(ro, nxt.reshape(cr, -1)).reshape(k, nxt.shape[1], nxt.shape[2])
+        for i in range(n - 1, b, -1):
+            cl, d, cr = A[i].shape
+            lo, ro, _, k, _ = self.svd(A[i].reshape(cl, d * cr), -1.0, 0, 1, 1)
+            A[i] = ro.reshape(k, d, cr)
+            prv = A[i - 1]
+            A[i - 1] = self.gemm(prv.reshape(-1, cl), lo).reshape(prv.shape[0], prv.shape[1], k)
+        theta = self.merge(A[b - 1].contiguous(), A[b].contiguous())
+        cl, d1, d2, cr = theta.shape
+        _, _, s, _, _ = self.svd(theta.reshape(cl * d1, d2 * cr), -1.0, 0, 1, 2)
+        return np.asarray(s, dtype=np.float64)
+
     def right_canonicalize(self, A):
         """Lossless right-to-left SVD pass: A[1:] right-orthonormal, the
         norm carried into A[0] (the gauge the TDVP sweep starts from)."""

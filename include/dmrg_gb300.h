@@ -110,10 +110,14 @@ int dmrg_heff_status(const dmrg_heff_t* op, void* work, size_t work_bytes, void*
  * precision must be DMRG_PREC_FP64 (else DMRG_ERR_UNSUPPORTED); an operator
  * whose dmrg_heff_workspace_bytes() exceeds DMRG_NOALLOC_SCRATCH_BYTES is
  * rejected with DMRG_ERR_WORKSPACE.  The first call on a device sets up the
- * array's address and should come before any stream capture.  All calls share
- * the array: calls that may execute at the same time race and must be
- * serialised by the caller (e.g. one stream); nothing in it needs to start
- * at zero. */
+ * array's address and should come before any stream capture; the address is
+ * cached per device number, so the library assumes the device's primary
+ * context (the CUDA runtime's) and no cudaDeviceReset between calls.  All
+ * calls share the array: calls that may execute at the same time race and
+ * must be serialised by the caller (e.g. one stream); nothing in it needs to
+ * start at zero.  The array is part of the library's device image: every
+ * device that loads the library holds its 64 MiB until the process exits,
+ * whether or not this entry point is called. */
 #define DMRG_NOALLOC_SCRATCH_BYTES (64u << 20)
 int dmrg_heff_apply_noalloc(const dmrg_heff_t* op, const void* x, void* y, void* stream);
 

@@ -51,6 +51,27 @@ def test_tf32x3_two_site_matvec(chil, chir, code):
     assert np.array_equal(y, y2)
 
 
+def test_tf32x3_two_site_matvec_at_the_headline_bond():
+    """The split-TF32 matvec at the headline bond (chi = 1024, d = 3, w = 5:
+    theta is 1024 x 3 x 3 x 1024) against the oracle's FP64 contraction on
+    the host, with the environments of a real state's scale replaced by
+    seeded Gaussian ones.  Bars: max|y - y_ref| <= 2e-6 max|y_ref| and
+    |y - y_ref| <= 1e-6 |y_ref|."""
+    rng = np.random.default_rng(1024)
+    Wi, Wj = _mpo_pair(3)
+    chi = 1024
+    L = rng.standard_normal((chi, Wi.shape[0], chi))
+    R = rng.standard_normal((chi, Wj.shape[3], chi))
+    th = rng.standard_normal((chi, 3, 3, chi))
+    ref = O.heff2_matvec(L, Wi, Wj, R, th).real
+    eng = _engine([Wi, Wj], "tf32x3")
+    Ld, Rd, thd = eng.to_device([L, R, th])
+    h = eng.heff2(Ld, eng.W[0], eng.W[1], Rd, th.shape)
+    y = eng.apply(h, thd).cpu().numpy()
+    assert np.max(np.abs(y - ref)) / np.max(np.abs(ref)) < TOL
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-6
+
+
 @pytest.mark.parametrize("m,k,n", [(300, 64, 200), (3 * 128, 256, 3 * 128), (5, 7, 9)])
 def test_tf32x3_gemm(m, k, n):
     rng = np.random.default_rng(m + k + n)

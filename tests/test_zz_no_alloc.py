@@ -1,6 +1,8 @@
 """dmrg_heff_apply_noalloc (scratch in a fixed device array inside the
 library) against dmrg_heff_apply (caller workspace) on the same operator:
-two calls in a row must both reproduce the workspace result.  The file name
+calls in a row must all reproduce the workspace result, and after the
+first one they must leave the device's free memory and torch's allocation
+unchanged.  The file name
 sorts last so the test also runs after every other GPU test, and it needs
 nothing from them when run alone."""
 import ctypes
@@ -59,13 +61,20 @@ def test_noalloc_matches_workspace_matvec_twice(kind, complex_):
     y_ref = torch.empty_like(x)
     _lib.check("dmrg_heff_apply", lib.dmrg_heff_apply(ctypes.byref(h), x.data_ptr(), y_ref.data_ptr(),
                                                       work.data_ptr(), need, stream))
-    outs = []
-    for _ in range(2):
-        y = torch.full_like(x, float("nan"))
+    outs = [torch.full_like(x, float("nan")) for _ in range(4)]
+    _lib.check("dmrg_heff_apply_noalloc", lib.dmrg_heff_apply_noalloc(ctypes.byref(h), x.data_ptr(),
+                                                                      outs[0].data_ptr(), stream))
+    torch.cuda.synchronize()
+    # after the first call (which looks up the array's address) the calls
+    # allocate nothing: neither torch's allocator nor the device's free
+    # memory moves
+    free0, allocated0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for y in outs[1:]:
         _lib.check("dmrg_heff_apply_noalloc", lib.dmrg_heff_apply_noalloc(ctypes.byref(h), x.data_ptr(),
                                                                           y.data_ptr(), stream))
-        outs.append(y)
     torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == allocated0
     scale = float(y_ref.abs().max())
     for y in outs:
         assert torch.isfinite(y).all()
