@@ -631,6 +631,143 @@ __global__ void __launch_bounds__(256) mpo_step_t_kernel(const float* __restrict
   }
 }
 
+// Tensor-core form of the same step for d1 d2 wl <= 48 and d1 d2 wr <= 48
+// (the S=1 bond: 45 x 45): per a' the step is the small GEMM
+// X3_a (out x b) = W2 (out x in) X1_a (in x b), run on legacy mma.sync
+// m16n8k8 TF32 tiles with the three split products (W2_hi X_hi + W2_hi X_lo
+// + W2_lo X_hi) accumulated in FP32.  The CUDA-core form above issues
+// 2025 FMAs and 506 shared loads per output column and sits at ~80% of the
+// SM's issue rate with the HBM at a quarter of its bandwidth; here a warp
+// covers one a' and 32 columns b (3 x 4 output tiles, 6 K steps, 216 MMAs),
+// W2 split once per CTA into shared memory.  Fragment layouts (PTX ISA,
+// mma.m16n8k8 .tf32): A a0 (g, t) a1 (g+8, t) a2 (g, t+4) a3 (g+8, t+4);
+// B b0 (t, g) b1 (t+4, g); C c0 (g, 2t) c1 (g, 2t+1) c2 (g+8, 2t)
+// c3 (g+8, 2t+1), with g = lane / 4 and t = lane % 4.
+constexpr int MMA_K = 48;            // padded in/out width
+constexpr int MMA_LD = MMA_K + 4;    // shared row pitch (floats)
+
+__device__ __forceinline__ void mma_tf32_16x8x8(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__global__ void __launch_bounds__(256, 3) mpo_step_mma_kernel(const float* __restrict__ X1T,
+                                                          const float* __restrict__ W2, int chil, int d1, int d2,
+                                                          int chir, int wl, int wr, int Kp, int pair_stores,
+                                                          float* __restrict__ hi, float* __restrict__ lo) {
+  // W2 hi/lo in fragment order: entry (mt * 6 + kt) * 32 + lane holds that
+  // lane's a0..a3 of m-tile mt, k-tile kt, so one 16-byte load per fragment
+  __shared__ float4 sAh[3 * 6 * 32];
+  __shared__ float4 sAl[3 * 6 * 32];
+  __shared__ int sOff[MMA_K];   // input column -> offset in X1T (-1: padding)
+  __shared__ int sOut[MMA_K];   // output row -> offset in the X3 row of a' (-1: padding)
+  const int nst = d1 * d2;
+  const int in_cols = nst * wl;
+  const int out_rows = nst * wr;
+  const long long ldt = (long long)nst * chir;
+  for (int i = threadIdx.x; i < 3 * 6 * 32; i += blockDim.x) {
+    const int f = i >> 5, l = i & 31;
+    const int mt = f / 6, kt = f - (f / 6) * 6;
+    const int r0 = 16 * mt + (l >> 2), c0 = 8 * kt + (l & 3);
+    float w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = r0 + (j & 1) * 8, c = c0 + (j >> 1) * 4;
+      w[j] = (r < out_rows && c < in_cols) ? W2[r * in_cols + c] : 0.f;
+    }
+    float4 h, q;
+    h.x = to_tf32(w[0]); q.x = to_tf32(w[0] - h.x);
+    h.y = to_tf32(w[1]); q.y = to_tf32(w[1] - h.y);
+    h.z = to_tf32(w[2]); q.z = to_tf32(w[2] - h.z);
+    h.w = to_tf32(w[3]); q.w = to_tf32(w[3] - h.w);
+    sAh[i] = h;
+    sAl[i] = q;
+  }
+  for (int c = threadIdx.x; c < MMA_K; c += blockDim.x) {
+    const int st = c / wl, k = c - (c / wl) * wl;
+    sOff[c] = c < in_cols ? (int)(k * ldt + (long long)st * chir) : -1;
+    const int sp_tp = c / wr, n = c - (c / wr) * wr;
+    sOut[c] = c < out_rows ? sp_tp * Kp + n * chir : -1;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const int a = blockIdx.y * RT_A + (threadIdx.x >> 5);
+  const int b0 = blockIdx.x * 32;
+  if (a >= chil) return;
+  const float* base = X1T + (long long)a * wl * ldt + b0;
+  float acc[3][4][4];
+#pragma unroll
+  for (int mt = 0; mt < 3; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[mt][nt][q] = 0.f;
+#pragma unroll 1
+  for (int kt = 0; kt < MMA_K / 8; ++kt) {
+    const int off0 = sOff[8 * kt + t], off1 = sOff[8 * kt + t + 4];
+    uint32_t bh[4][2], bl[4][2];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+      const int col = 8 * nt + g;
+      const bool ok = b0 + col < chir;
+      const float x0 = (ok && off0 >= 0) ? base[off0 + col] : 0.f;
+      const float x1 = (ok && off1 >= 0) ? base[off1 + col] : 0.f;
+      const float h0 = to_tf32(x0), h1 = to_tf32(x1);
+      bh[nt][0] = __float_as_uint(h0);
+      bh[nt][1] = __float_as_uint(h1);
+      bl[nt][0] = __float_as_uint(to_tf32(x0 - h0));
+      bl[nt][1] = __float_as_uint(to_tf32(x1 - h1));
+    }
+#pragma unroll
+    for (int mt = 0; mt < 3; ++mt) {
+      const float4 fh = sAh[(mt * 6 + kt) * 32 + lane];
+      const float4 fl = sAl[(mt * 6 + kt) * 32 + lane];
+      const uint32_t ah[4] = {__float_as_uint(fh.x), __float_as_uint(fh.y), __float_as_uint(fh.z),
+                              __float_as_uint(fh.w)};
+      const uint32_t al[4] = {__float_as_uint(fl.x), __float_as_uint(fl.y), __float_as_uint(fl.z),
+                              __float_as_uint(fl.w)};
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        mma_tf32_16x8x8(acc[mt][nt], ah, bh[nt][0], bh[nt][1]);
+        mma_tf32_16x8x8(acc[mt][nt], ah, bl[nt][0], bl[nt][1]);
+        mma_tf32_16x8x8(acc[mt][nt], al, bh[nt][0], bh[nt][1]);
+      }
+    }
+  }
+  // c0/c1 (and c2/c3) are neighbouring columns b, b + 1 of one output row
+  const long long arow = (long long)a * nst * Kp;
+#pragma unroll
+  for (int mt = 0; mt < 3; ++mt)
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int ro = sOut[16 * mt + g + 8 * half];
+      if (ro < 0) continue;
+#pragma unroll
+      for (int nt = 0; nt < 4; ++nt) {
+        const int b = b0 + 8 * nt + 2 * t;
+        if (b >= chir) continue;
+        const long long o = arow + ro + b;
+        const float v0 = acc[mt][nt][2 * half], v1 = acc[mt][nt][2 * half + 1];
+        const float h0 = to_tf32(v0), h1 = to_tf32(v1);
+        if (pair_stores && b + 1 < chir) {
+          *reinterpret_cast<float2*>(hi + o) = make_float2(h0, h1);
+          *reinterpret_cast<float2*>(lo + o) = make_float2(to_tf32(v0 - h0), to_tf32(v1 - h1));
+        } else {
+          hi[o] = h0;
+          lo[o] = to_tf32(v0 - h0);
+          if (b + 1 < chir) {
+            hi[o + 1] = h1;
+            lo[o + 1] = to_tf32(v1 - h1);
+          }
+        }
+      }
+    }
+}
+
 inline int egrid(long long n) {
   long long g = (n + 255) / 256;
   if (g > 152 * 16) g = 152 * 16;
@@ -908,6 +1045,17 @@ int launch_mpo_step_t(const Heff2Plan& p, cudaStream_t s) {
   return DMRG_OK;
 }
 
+int launch_mpo_step_mma(const Heff2Plan& p, cudaStream_t s) {
+  dim3 grid((p.cr + 31) / 32, (p.cl + RT_A - 1) / RT_A);
+  if (grid.y > 65535) return DMRG_ERR_ARG;
+  // paired 8-byte stores need even offsets: chir, Kp even and 8-byte aligned bases
+  const int pair = ((p.cr | p.Kp4) & 1) == 0 && (reinterpret_cast<uintptr_t>(p.X3_hi) & 7) == 0 &&
+                   (reinterpret_cast<uintptr_t>(p.X3_lo) & 7) == 0;
+  mpo_step_mma_kernel<<<grid, 256, 0, s>>>(p.X1, p.W2, p.cl, p.d1, p.d2, p.cr, p.wl, p.wr, p.Kp4, pair, p.X3_hi,
+                                           p.X3_lo);
+  DMRG_CHECK_LAUNCH();
+  return DMRG_OK;
+}
 
 }  // namespace
 
@@ -977,7 +1125,8 @@ int tf32x3_heff_apply_prepared(const dmrg_heff_t& o, const double* x, double* y,
     // coalesce across lanes (consecutive rows) and so do the MPO step's loads
     GemmOut g1{p.X1, 1, p.M1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
     DMRG_TRY(gemm_split(p.thT_hi, p.thT_lo, p.L_hi, p.L_lo, (int)p.M1, (int)p.N1, p.Kp1, g1, p.err, s));
-    if (in_cols <= 48) DMRG_TRY(launch_mpo_step_t<48>(p, s));
+    if (in_cols <= MMA_K && nst * p.wr <= MMA_K) DMRG_TRY(launch_mpo_step_mma(p, s));
+    else if (in_cols <= 48) DMRG_TRY(launch_mpo_step_t<48>(p, s));
     else DMRG_TRY(launch_mpo_step_t<96>(p, s));
   } else {
     GemmOut g1{p.X1, p.N1, 1, (int)p.M1, (int)p.N1, 0, 0, 1.f};
