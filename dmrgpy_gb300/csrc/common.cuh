@@ -174,4 +174,27 @@ template <typename T> int vfill_random(T* x, long long n, unsigned long long see
 template <typename T> int gemv_sub(const T* Q, long long ldq, int k, const T* h, T* w, long long n, int overwrite, cudaStream_t s);
 int nan_check(const void* x, long long n_doubles, int* flag, cudaStream_t s);
 
+// FP64 value of an FP32 one from its bit pattern (exact; zero, subnormal,
+// inf and nan take the conversion), keeping the FP64 pipe free in the
+// epilogues that widen FP32 accumulators
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t ef = (u >> 23) & 0xffu;
+  if (ef == 0u || ef == 0xffu) return static_cast<double>(f);
+  return __hiloint2double(static_cast<int>((u & 0x80000000u) | ((ef + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
+                          static_cast<int>(u << 29));
+}
+
+// FP32 value of an FP64 one (round half away from zero at 24 bits) from its
+// bit pattern; values outside the FP32 normal range take the conversion
+__device__ __forceinline__ float narrow(double x) {
+  const uint32_t xh = static_cast<uint32_t>(__double2hiint(x));
+  const uint32_t xl = static_cast<uint32_t>(__double2loint(x));
+  const int e = static_cast<int>((xh >> 20) & 0x7ffu);
+  if (e < 897 || e > 1150) return static_cast<float>(x);
+  const uint32_t frac = ((xh & 0xfffffu) << 3) | (xl >> 29);   // 23 fraction bits
+  // a carry out of the fraction moves into the exponent field (to inf past the top)
+  return __uint_as_float((xh & 0x80000000u) | ((static_cast<uint32_t>(e - 896) << 23) + frac + ((xl >> 28) & 1u)));
+}
+
 }  // namespace dmrg

@@ -61,15 +61,6 @@ __global__ void copy2d_kernel(const double* __restrict__ src, long long lds, dou
   }
 }
 
-__global__ void copy_scaled_kernel(const double* __restrict__ src, long long lds, double* __restrict__ dst,
-                                   long long ldd, int rows, int cols, double a) {
-  const long long total = (long long)rows * cols;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    const int r = (int)(i / cols), c = (int)(i % cols);
-    dst[(long long)r * ldd + c] = a * src[(long long)r * lds + c];
-  }
-}
-
 __global__ void sumsq_kernel(const double* __restrict__ x, long long n, double* __restrict__ out) {
   __shared__ double sh[32];
   double s = 0.0;
@@ -90,13 +81,6 @@ inline int egrid(long long n) {
   if (g > 152 * 8) g = 152 * 8;
   if (g < 1) g = 1;
   return (int)g;
-}
-
-int copy_scaled(const double* src, long long lds, double* dst, long long ldd, int rows, int cols, double a,
-                cudaStream_t s) {
-  copy_scaled_kernel<<<egrid((long long)rows * cols), 256, 0, s>>>(src, lds, dst, ldd, rows, cols, a);
-  DMRG_CHECK_LAUNCH();
-  return DMRG_OK;
 }
 
 // dst (cols x rows, ld = ldd) = src^T, src rows x cols with leading dim lds
@@ -179,8 +163,9 @@ __global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ 
 
 // B = b*A + c*I  (k x k), also reports max|A - I| into *dev.  A block
 // covers POLY_ROWS whole rows, so the grid ends in k / POLY_ROWS atomics on
-// *dev (one per block), not one per 256 elements.
-constexpr int POLY_ROWS = 8;
+// *dev (one per block), not one per 256 elements; one row per block gives
+// k blocks, enough to spread a 1024 x 1024 matrix over every SM.
+constexpr int POLY_ROWS = 1;
 __global__ void poly_kernel(const double* __restrict__ A, int k, double b, double c, double* __restrict__ B,
                             unsigned long long* __restrict__ dev) {
   double mx = 0.0;
@@ -207,11 +192,14 @@ __global__ void poly_kernel(const double* __restrict__ A, int k, double b, doubl
 }
 
 // FP16 operand pair of x * scale (scale a power of two that keeps |x scale|
-// inside the FP16 range): hi = fp16(x s), lo = fp16(x s - hi)
-__device__ __forceinline__ void split_h(double x, double scale, __half& hi, __half& lo) {
-  const double v = x * scale;
-  hi = __double2half(v);
-  lo = __double2half(v - static_cast<double>(__half2float(hi)));
+// inside the FP16 range): hi = fp16(x s), lo = fp16(x s - hi).  Computed in
+// FP32 from x rounded to FP32 (the pair resolves 22 bits, FP32 holds 24):
+// FP64 arithmetic and conversions run at a small fraction of the FP32 rate
+// on GB300.
+__device__ __forceinline__ void split_h(float x, float scale, __half& hi, __half& lo) {
+  const float v = x * scale;
+  hi = __float2half_rn(v);
+  lo = __float2half_rn(v - __half2float(hi));
 }
 
 // B = b*A + c*I (k x k) stored as the FP16 operand pair [r][Kk] (scaled) of
@@ -219,14 +207,16 @@ __device__ __forceinline__ void split_h(double x, double scale, __half& hi, __ha
 __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, double scale,
                                   __half* __restrict__ hi, __half* __restrict__ lo, int Kk,
                                   unsigned long long* __restrict__ dev) {
-  // POLY_ROWS whole rows per block (one atomic per block)
+  // POLY_ROWS whole rows per block (one atomic per block); FP32 arithmetic
+  // (A carries the FP32-level accuracy of the split products)
+  const float bf = static_cast<float>(b), cf = static_cast<float>(c), sf = static_cast<float>(scale);
   double mx = 0.0;
   for (int r = blockIdx.y * POLY_ROWS; r < k && r < (blockIdx.y + 1) * POLY_ROWS; ++r)
     for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
-      const double a = A[(long long)r * k + cc];
-      split_h(b * a + (r == cc ? c : 0.0), scale, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
-      const double dv = fabs(a - (r == cc ? 1.0 : 0.0));
-      mx = dv <= mx ? mx : (dv == dv ? dv : INFINITY);   // a non-finite entry reports +inf
+      const float a = narrow(A[(long long)r * k + cc]);
+      split_h(fmaf(bf, a, r == cc ? cf : 0.f), sf, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
+      const float dv = fabsf(a - (r == cc ? 1.f : 0.f));
+      if (!(dv <= mx)) mx = dv == dv ? static_cast<double>(dv) : INFINITY;   // a non-finite entry reports +inf
     }
   __shared__ double red[32];
 #pragma unroll
@@ -246,23 +236,36 @@ __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b,
 __global__ void split_both_kernel(const double* __restrict__ X, long long ld, int m, int k, int Km, int Kk,
                                   double scale, __half* __restrict__ xr_hi, __half* __restrict__ xr_lo,
                                   __half* __restrict__ xt_hi, __half* __restrict__ xt_lo) {
-  __shared__ double t[32][33];
+  __shared__ float t[32][33];
   const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const float sf = static_cast<float>(scale);
   for (int j = ty; j < 32; j += 8) {
     const int r = r0 + j, c = c0 + tx;
-    const double v = (r < m && c < k) ? X[(long long)r * ld + c] : 0.0;
+    const float v = (r < m && c < k) ? narrow(X[(long long)r * ld + c]) : 0.f;
     t[j][tx] = v;
-    if (r < m && c < Kk) split_h(v, scale, xr_hi[(long long)r * Kk + c], xr_lo[(long long)r * Kk + c]);
+    if (r < m && c < Kk) split_h(v, sf, xr_hi[(long long)r * Kk + c], xr_lo[(long long)r * Kk + c]);
   }
   __syncthreads();
   for (int j = ty; j < 32; j += 8) {
     const int c = c0 + j, r = r0 + tx;
-    if (c < k && r < Km) split_h(t[tx][j], scale, xt_hi[(long long)c * Km + r], xt_lo[(long long)c * Km + r]);
+    if (c < k && r < Km) split_h(t[tx][j], sf, xt_hi[(long long)c * Km + r], xt_lo[(long long)c * Km + r]);
   }
 }
 
 inline int pad64s(long long x) { return (int)((x + 63) / 64 * 64); }
+
+// X (m x k, ld) = (hi + lo) / scale from the row-major FP16 operand pair of
+// the polar iterate ([r][Kk])
+__global__ void pair_to_f64_kernel(const __half* __restrict__ hi, const __half* __restrict__ lo, int Kk, int m, int k,
+                                   float inv_scale, double* __restrict__ X, long long ld) {
+  const long long total = (long long)m * k;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i / k), c = (int)(i - (i / k) * k);
+    const long long o = (long long)r * Kk + c;
+    X[(long long)r * ld + c] = widen((__half2float(hi[o]) + __half2float(lo[o])) * inv_scale);
+  }
+}
 
 // FP16 operand arrays of the polar iteration ([rows][K] pairs of scaled
 // values, K padded to 64):
@@ -344,9 +347,8 @@ int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, d
   return DMRG_OK;
 }
 
-int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, double* B, double* n2,
-               unsigned long long* dev, void* gw, size_t gw_bytes, void* splits, int* err, bool exact,
-               cudaStream_t s) {
+int orth_polar(double* Z, long long ld, int m, int k, double* A, double* B, double* n2, unsigned long long* dev,
+               void* gw, size_t gw_bytes, void* splits, int* err, bool exact, cudaStream_t s) {
   const int Km = pad64s(m), Kk = pad64s(k);
   const PolarSplits ps = polar_splits(splits, m, k);
   // the K padding of the split arrays must read as zero
@@ -373,24 +375,27 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
   DMRG_CHECK_LAUNCH();
   col_factor_kernel<<<(k + 255) / 256, 256, 0, s>>>(n2, k, 1.0 / sqrt((double)k));
   DMRG_CHECK_LAUNCH();
-  scale_perturb_kernel<<<dim3((k + 255) / 256, m), 256, 0, s>>>(Z, ld, k, n2, 1e-8 / sqrt((double)m),
+  // the perturbation (spectral norm ~5e-8) stays below the rounding of the
+  // FP16 operand pairs (~2.4e-7 of |X|), so it adds no error of its own
+  scale_perturb_kernel<<<dim3((k + 255) / 256, m), 256, 0, s>>>(Z, ld, k, n2, 1e-7 / sqrt((double)m),
                                                                 0x5eed5ull + (unsigned)k);
   DMRG_CHECK_LAUNCH();
   split_both_kernel<<<sgrid, 256, 0, s>>>(Z, ld, m, k, Km, Kk, SX, ps.xr_hi[0], ps.xr_lo[0], ps.xt_hi, ps.xt_lo);
   DMRG_CHECK_LAUNCH();
-  double* X = Z;
-  double* Y = X2;
   int cur = 0;
-  // 14 quintic steps lift a direction from the 1e-8 perturbation level to
-  // ~0.3; the cubic steps then converge quadratically
+  // 14 quintic steps (3.4x per step for small singular values) lift a
+  // direction from the ~2e-8 perturbation level into the band [0.7, 1.2];
+  // a few cubic steps then converge quadratically.  The iterates live only
+  // as their FP16 operand pairs (written by each X B epilogue); the FP64
+  // basis is formed once from the final pair.
   const int quintic = 14, cubic_max = 16;
   double d = 1.0;
   for (int it = 0; it < quintic + cubic_max; ++it) {
     const bool q = it < quintic;
     DMRG_TRY(gram(q));
-    // Y = X B, written with the next iterate's two splits
+    // X B, written as the next iterate's two splits only
     GemmOut xb{};
-    xb.C = Y; xb.ldm = ld; xb.ldn = 1; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = (float)(1.0 / (SX * SB));
+    xb.C = nullptr; xb.M = m; xb.N = k; xb.out_f64 = 1; xb.alpha = (float)(1.0 / (SX * SB));
     xb.rhi = ps.xr_hi[1 - cur]; xb.rlo = ps.xr_lo[1 - cur]; xb.rld = Kk;
     xb.thi = ps.xt_hi; xb.tlo = ps.xt_lo; xb.tld = Km; xb.split_scale = SX;
     if (q) {
@@ -416,12 +421,11 @@ int orth_polar(double* Z, long long ld, int m, int k, double* X2, double* A, dou
       if (d < 5e-6) break;
     }
     DMRG_TRY(f16x3_gemm_split(ps.xr_hi[cur], ps.xr_lo[cur], ps.bs_hi, ps.bs_lo, m, k, Kk, xb, err, s));
-    double* t = X;
-    X = Y;
-    Y = t;
     cur = 1 - cur;
   }
-  if (X != Z) DMRG_TRY(copy_scaled(X, ld, Z, ld, m, k, 1.0, s));
+  pair_to_f64_kernel<<<egrid((long long)m * k), 256, 0, s>>>(ps.xr_hi[cur], ps.xr_lo[cur], Kk, m, k,
+                                                              (float)(1.0 / SX), Z, ld);
+  DMRG_CHECK_LAUNCH();
   // a basis still far from orthonormal (a direction below the perturbation
   // level, or a non-finite value) is reported instead of being corrected:
   // the caller falls back to the FP64 SVD
@@ -442,7 +446,7 @@ size_t gemm_scratch_bytes(int big) {
 size_t subspace_workspace_bytes(int m, int n, int k) {
   const size_t big = (size_t)(m > n ? m : n);
   const size_t d = sizeof(double);
-  return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 5 * align_up(d * big * k, 1024) +
+  return align_up(256, 1024) + align_up(d * (size_t)m * n, 1024) + 3 * align_up(d * big * k, 1024) +
          2 * align_up(d * (size_t)k * k, 1024) + align_up(d * k, 1024) +
          gemm_scratch_bytes((int)big) + polar_split_bytes((int)big, k) + align_up(64, 1024);
 }
@@ -472,7 +476,6 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   double* S = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* Y = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* C = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
-  double* PX = reinterpret_cast<double*>(p); p += align_up(d * big * k, 1024);
   double* PA = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* PB_ = reinterpret_cast<double*>(p); p += align_up(d * (size_t)k * k, 1024);
   double* Pn2 = reinterpret_cast<double*>(p); p += align_up(d * k, 1024);
@@ -485,7 +488,7 @@ int subspace_truncate(int m, int n, int k, const double* theta, const double* X,
   DMRG_CUDA_TRY(cudaMemsetAsync(err, 0, 256, s));
   DMRG_CUDA_TRY(cudaMemsetAsync(acc, 0, 64, s));
   auto orth = [&](double* Zp, int rows, bool exact) -> int {
-    return orth_polar(Zp, k, rows, k, PX, PA, PB_, Pn2, pdev, gw, gw_bytes, splits, err, exact, s);
+    return orth_polar(Zp, k, rows, k, PA, PB_, Pn2, pdev, gw, gw_bytes, splits, err, exact, s);
   };
 
   // canonical problem: keep the left basis of Th (M x N); W (N x k) is an

@@ -60,9 +60,32 @@ constexpr int gemm_smem_bytes(int bnt) {
 }
 constexpr int GEMM_THREADS = 192;           // 6 warps
 
+// TF32 pair of an FP64 value: hi = x rounded to 11 significant bits, lo =
+// (x - hi) rounded to 11 bits.  Built from the bit pattern with integer and
+// FP32 operations: GB300 issues FP64 arithmetic and FP64 <-> FP32
+// conversions at a small fraction of the FP32 rate, and the split of a
+// chi=1024 two-site tensor (9.4M values) through them took ~70 us.  Values
+// whose parts leave the FP32 normal range (|x| < 2^-126 or |x| >= 2^115,
+// zero, inf, nan) take the conversion route.
 __device__ __forceinline__ void split2(double x, float& hi, float& lo) {
-  hi = to_tf32(static_cast<float>(x));
-  lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
+  const uint32_t xh = static_cast<uint32_t>(__double2hiint(x));
+  const uint32_t xl = static_cast<uint32_t>(__double2loint(x));
+  const int e = static_cast<int>((xh >> 20) & 0x7ffu);   // biased FP64 exponent
+  if (e < 897 || e > 1138) {
+    hi = to_tf32(static_cast<float>(x));
+    lo = to_tf32(static_cast<float>(x - static_cast<double>(hi)));
+    return;
+  }
+  const uint32_t sgn = xh & 0x80000000u;
+  const uint32_t mh = xh & 0xfffffu;        // fraction bits 51..32
+  const uint32_t up = (mh >> 9) & 1u;       // round half away at fraction bit 41
+  // a carry out of the 10 fraction bits moves into the exponent field
+  hi = __uint_as_float(sgn | ((static_cast<uint32_t>(e - 896) << 23) + (((mh >> 10) + up) << 13)));
+  // x - hi = (rh 2^32 + xl) 2^(e - 1075) with |rh 2^32 + xl| <= 2^41
+  const int rh = static_cast<int>(mh & 0x3ffu) - static_cast<int>(up << 10);
+  const float r = fmaf(static_cast<float>(rh), 4294967296.0f, static_cast<float>(xl));
+  const float v = r * 5.42101086242752217e-20f * __uint_as_float(static_cast<uint32_t>(e - 884) << 23);
+  lo = to_tf32(sgn ? -v : v);
 }
 
 // FP16 pair of x * scale (scale a power of two chosen so that |x * scale|
@@ -71,6 +94,19 @@ __device__ __forceinline__ void split2h(double x, double scale, __half& hi, __ha
   const double v = x * scale;
   hi = __double2half(v);
   lo = __double2half(v - static_cast<double>(__half2float(hi)));
+}
+
+// the same pairs of an FP32 value (scale a power of two): x s - hi is exact
+// in FP32, so the pair matches the FP64 route up to ties
+__device__ __forceinline__ void split2h(float x, float scale, __half& hi, __half& lo) {
+  const float v = x * scale;
+  hi = __float2half_rn(v);
+  lo = __float2half_rn(v - __half2float(hi));
+}
+
+__device__ __forceinline__ void split2(float x, float& hi, float& lo) {
+  hi = to_tf32(x);
+  lo = to_tf32(x - hi);
 }
 
 // Epilogue of the polar-iteration GEMMs (GemmOut with split outputs, a
@@ -89,11 +125,26 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
   // 4 split values per store: 16 bytes (tf32 pairs) or 8 bytes (fp16)
   const bool rvec = full && out.rhi && ((reinterpret_cast<uintptr_t>(out.rhi) & 15) == 0) &&
                     ((reinterpret_cast<uintptr_t>(out.rlo) & 15) == 0) && out.rld % 4 == 0;
+  // FP64 values only where they carry more than the FP32 accumulator: an
+  // accumulated C, or a diagonal term added to a stored C.  Otherwise the
+  // value, its C copy and its splits come from FP32 arithmetic (the FP64
+  // pipe of GB300 would otherwise bound this epilogue).
+  const bool wide = out.accumulate || (C && out.diag != 0.0);
+  const float diagf = static_cast<float>(out.diag);
+  const float scalef = static_cast<float>(out.split_scale);
 #pragma unroll
   for (int c = 0; c < BNT; c += 4) {
     double v[4];
+    float vf[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = static_cast<double>(out.alpha * acc[c + j]) + (n0 + c + j == gm ? out.diag : 0.0);
+    for (int j = 0; j < 4; ++j) {
+      if (wide) {
+        v[j] = static_cast<double>(out.alpha * acc[c + j]) + (n0 + c + j == gm ? out.diag : 0.0);
+      } else {
+        vf[j] = out.alpha * acc[c + j] + (n0 + c + j == gm ? diagf : 0.f);
+        v[j] = widen(vf[j]);
+      }
+    }
     if (C) {
       if (cvec) {
         double2* p = reinterpret_cast<double2*>(C + crow + n0 + c);
@@ -119,7 +170,10 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
       if constexpr (F16) {
         __half h[4], l[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) split2h(v[j], out.split_scale, h[j], l[j]);
+        for (int j = 0; j < 4; ++j) {
+          if (wide) split2h(v[j], out.split_scale, h[j], l[j]);
+          else split2h(vf[j], scalef, h[j], l[j]);
+        }
         if (out.rhi) {
           __half* ph = static_cast<__half*>(out.rhi) + (long long)gm * out.rld + n0 + c;
           __half* pl = static_cast<__half*>(out.rlo) + (long long)gm * out.rld + n0 + c;
@@ -153,7 +207,10 @@ __device__ __forceinline__ void store_extra(const float* acc, const GemmOut& out
       } else {
         float h[4], l[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) split2(v[j], h[j], l[j]);
+        for (int j = 0; j < 4; ++j) {
+          if (wide) split2(v[j], h[j], l[j]);
+          else split2(vf[j], h[j], l[j]);
+        }
         if (out.rhi) {
           float* ph = static_cast<float*>(out.rhi) + (long long)gm * out.rld + n0 + c;
           float* pl = static_cast<float*>(out.rlo) + (long long)gm * out.rld + n0 + c;
@@ -355,9 +412,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
       int m0, n0;
       tile_origin(t, tiles_m, tiles_n, group, BNT, m0, n0);
-      float acc[BNT];
+      // column pairs in 64-bit registers, summed with packed FP32 adds
+      // (round to nearest per lane, as the scalar add): half the add
+      // instructions, which share their issue slots with the MMA warp on one
+      // SM sub-partition
+      uint64_t acc2[BNT / 2];
 #pragma unroll
-      for (int c = 0; c < BNT; ++c) acc[c] = 0.f;
+      for (int c = 0; c < BNT / 2; ++c) acc2[c] = 0ull;
       for (int kt = 0; kt < KT * SUB && ok; ++kt, ++g) {
         const int b = (int)(g % NACC);
         const long long u = g / NACC;
@@ -366,16 +427,19 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         if (ok) {
 #pragma unroll
           for (int c = 0; c < ACC_COLS; c += 64) {
-            float v[64];
-            tmem_ld64(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * ACC_COLS + c, v);
+            uint32_t v[64];
+            tmem_ld64u(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * ACC_COLS + c, v);
 #pragma unroll
-            for (int j = 0; j < 64; ++j) acc[(c + j) % BNT] += v[j];
+            for (int j = 0; j < 64; j += 2) add_f32x2(acc2[((c + j) % BNT) / 2], v[j], v[j + 1]);
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
       }
+      float acc[BNT];
+#pragma unroll
+      for (int c = 0; c < BNT / 2; ++c) unpack_f32x2(acc2[c], acc[2 * c], acc[2 * c + 1]);
       if (!ok) break;
       const int gm = m0 + row;
       if constexpr (EXTRA) {
@@ -410,7 +474,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           if (vec) {
             if (out.out_f64) {
               double2* p = reinterpret_cast<double2*>(static_cast<double*>(out.C) + rowoff + n0 + c);
-              double2 u = make_double2(r0, r1), v = make_double2(r2, r3);
+              double2 u = make_double2(widen(r0), widen(r1)), v = make_double2(widen(r2), widen(r3));
               if (out.accumulate) {
                 const double2 pu = p[0], pv = p[1];
                 u.x += pu.x; u.y += pu.y; v.x += pv.x; v.y += pv.y;
@@ -435,7 +499,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 const long long o = rowoff + (long long)gn * out.ldn;
                 if (out.out_f64) {
                   double* C = static_cast<double*>(out.C);
-                  C[o] = out.accumulate ? C[o] + (double)rr[j] : (double)rr[j];
+                  C[o] = out.accumulate ? C[o] + widen(rr[j]) : widen(rr[j]);
                 } else {
                   float* C = static_cast<float*>(out.C);
                   C[o] = out.accumulate ? C[o] + rr[j] : rr[j];
@@ -644,7 +708,6 @@ __global__ void __launch_bounds__(256) mpo_step_t_kernel(const float* __restrict
 // B b0 (t, g) b1 (t+4, g); C c0 (g, 2t) c1 (g, 2t+1) c2 (g+8, 2t)
 // c3 (g+8, 2t+1), with g = lane / 4 and t = lane % 4.
 constexpr int MMA_K = 48;            // padded in/out width
-constexpr int MMA_LD = MMA_K + 4;    // shared row pitch (floats)
 
 __device__ __forceinline__ void mma_tf32_16x8x8(float* c, const uint32_t* a, uint32_t b0, uint32_t b1) {
   asm volatile(
