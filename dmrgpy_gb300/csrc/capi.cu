@@ -171,7 +171,7 @@ struct KrylovWs {
   void* w;        // n
   void* hdev;     // kcap (T)
   double* sc;     // scalars: [0] alpha (T: 2 doubles) [2] beta [3] beta_prev [4] norm
-  double* part;   // multidot partials 2 * 64 * kcap
+  double* part;   // multidot partials 2 * MULTIDOT_MAX_GRID * kcap
   double* red;    // reduction scratch: 8 + 2*RB
   void* hw;       // heff workspace
 };
@@ -191,7 +191,7 @@ size_t krylov_ws(const dmrg_heff_t* o, int kcap, KrylovWs* out, void* base) {
   w.w = take(n * es);
   w.hdev = take((size_t)kcap * es);
   w.sc = static_cast<double*>(take(16 * sizeof(double)));
-  w.part = static_cast<double*>(take(2 * 64 * (size_t)kcap * sizeof(double)));
+  w.part = static_cast<double*>(take(2 * (size_t)MULTIDOT_MAX_GRID * kcap * sizeof(double)));
   w.red = static_cast<double*>(take((8 + 2 * 2 * 152) * sizeof(double)));
   w.hw = take(heff_ws(o));
   if (out) *out = w;

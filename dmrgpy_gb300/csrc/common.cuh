@@ -168,6 +168,9 @@ template <typename T> int vdot(const T* x, const T* y, long long n, T* out, doub
 template <typename T> int vnorm(const T* x, long long n, double* out, double* scratch, cudaStream_t s);
 template <typename T> int vscale_dev_inv(T* y, const T* x, const double* denom, long long n, cudaStream_t s);
 template <typename T> int vscale(T* x, T a, long long n, cudaStream_t s);
+// CTAs per vector of the block dot products h = Q^H w (two per SM); the
+// caller's partial scratch holds 2 * MULTIDOT_MAX_GRID doubles per vector
+constexpr int MULTIDOT_MAX_GRID = 2 * 152;
 template <typename T> int vcopy(T* y, const T* x, long long n, cudaStream_t s);
 template <typename T> int vfill_random(T* x, long long n, unsigned long long seed, cudaStream_t s);
 // w = w - Q h (or w = Q h when overwrite); Q column-major n x k, leading dim ldq

@@ -141,6 +141,24 @@ __device__ __forceinline__ void tmem_ld64u(uint32_t taddr, uint32_t* r) {
       : "memory");
 }
 
+// 32 consecutive FP32 columns of this warp's 32 TMEM lanes, raw bits
+__device__ __forceinline__ void tmem_ld32u(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
+
+// N consecutive FP32 columns (N = 32 or 64), one load and one wait
+template <int N>
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t* r) {
+  static_assert(N == 32 || N == 64, "tmem_ld_cols: 32 or 64 columns");
+  if constexpr (N == 64) tmem_ld64u(taddr, r);
+  else tmem_ld32u(taddr, r);
+}
+
 // acc (two FP32 lanes in 64 bits) += (lo, hi), one packed add
 __device__ __forceinline__ void add_f32x2(uint64_t& acc, uint32_t lo, uint32_t hi) {
   asm("{\n\t.reg .b64 t;\n\tmov.b64 t, {%1, %2};\n\tadd.rn.f32x2 %0, %0, t;\n\t}" : "+l"(acc) : "r"(lo), "r"(hi));

@@ -58,7 +58,7 @@ constexpr int TILE_A_BYTES = BM * BK * 4;   // 16 KB
 constexpr int gemm_smem_bytes(int bnt) {
   return (bnt == 64 ? 4 : 3) * (2 * TILE_A_BYTES + 2 * bnt * BK * 4) + 1024 + 256;
 }
-constexpr int GEMM_THREADS = 192;           // 6 warps
+constexpr int GEMM_THREADS = 320;           // 10 warps: TMA producer, MMA issuer, 8 epilogue
 
 // TF32 pair of an FP64 value: hi = x rounded to 11 significant bits, lo =
 // (x - hi) rounded to 11 bits.  Built from the bit pattern with integer and
@@ -301,7 +301,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     }
     for (int b = 0; b < NACC; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+      mbar_init(&acc_empty[b], 8);  // one arrival per epilogue warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -404,46 +404,55 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       }
     }
   } else {
-    // epilogue: warps 2..5 -> TMEM lane quarter (warp % 4); one row per thread
+    // epilogue: warps 2..9.  A warp reaches only the TMEM lane quarter
+    // warp % 4, so two warps share each quarter (one row per thread) and
+    // split the tile's columns: warps 2..5 the first BNT / 2, warps 6..9 the
+    // rest.  Each K-slice buffer is thus drained by two warps in parallel,
+    // and each warp stores half of the tile.
+    constexpr int HB = BNT / 2;
     const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
     const int row = q * 32 + lane;
     long long g = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      int m0, n0;
-      tile_origin(t, tiles_m, tiles_n, group, BNT, m0, n0);
+      int m0, n0t;
+      tile_origin(t, tiles_m, tiles_n, group, BNT, m0, n0t);
+      const int n0 = n0t + half * HB;   // first output column of this warp
       // column pairs in 64-bit registers, summed with packed FP32 adds
       // (round to nearest per lane, as the scalar add): half the add
       // instructions, which share their issue slots with the MMA warp on one
       // SM sub-partition
-      uint64_t acc2[BNT / 2];
+      uint64_t acc2[HB / 2];
 #pragma unroll
-      for (int c = 0; c < BNT / 2; ++c) acc2[c] = 0ull;
+      for (int c = 0; c < HB / 2; ++c) acc2[c] = 0ull;
       for (int kt = 0; kt < KT * SUB && ok; ++kt, ++g) {
         const int b = (int)(g % NACC);
         const long long u = g / NACC;
         ok = mbar_wait(&acc_full[b], (uint32_t)(u & 1), err);
         tc_fence_after();
         if (ok) {
+          // MERGE buffers hold A_hi.B_hi (+ A_lo.B_hi) in columns [0, BNT)
+          // and A_hi.B_lo in [BNT, 2 BNT): both halves add into acc
 #pragma unroll
-          for (int c = 0; c < ACC_COLS; c += 64) {
-            uint32_t v[64];
-            tmem_ld64u(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * ACC_COLS + c, v);
+          for (int grp = 0; grp < ACC_COLS / BNT; ++grp) {
+            uint32_t v[HB];
+            tmem_ld_cols<HB>(tmem + (static_cast<uint32_t>(q * 32) << 16) + b * ACC_COLS + grp * BNT + half * HB, v);
 #pragma unroll
-            for (int j = 0; j < 64; j += 2) add_f32x2(acc2[((c + j) % BNT) / 2], v[j], v[j + 1]);
+            for (int j = 0; j < HB; j += 2) add_f32x2(acc2[j / 2], v[j], v[j + 1]);
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
       }
-      float acc[BNT];
+      float acc[HB];
 #pragma unroll
-      for (int c = 0; c < BNT / 2; ++c) unpack_f32x2(acc2[c], acc[2 * c], acc[2 * c + 1]);
+      for (int c = 0; c < HB / 2; ++c) unpack_f32x2(acc2[c], acc[2 * c], acc[2 * c + 1]);
       if (!ok) break;
       const int gm = m0 + row;
       if constexpr (EXTRA) {
-        if (gm < out.M) store_extra<BNT, F16>(acc, out, gm, n0);
+        if (gm < out.M) store_extra<HB, F16>(acc, out, gm, n0);
       } else {
       // full-width tiles of row-contiguous outputs are written with 16-byte
       // stores (4 floats / 2+2 doubles per step) instead of one element
@@ -453,22 +462,22 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       const bool tstore = inrow && out.ldm == 1 && !out.out_f64 && !out.accumulate;
       if (tstore) {
         float* pc = static_cast<float*>(out.C) + gm + (long long)n0 * out.ldn;
-        if (n0 + BNT <= out.N) {
+        if (n0 + HB <= out.N) {
 #pragma unroll
-          for (int c = 0; c < BNT; ++c) pc[(long long)c * out.ldn] = out.alpha * acc[c];
+          for (int c = 0; c < HB; ++c) pc[(long long)c * out.ldn] = out.alpha * acc[c];
         } else {
 #pragma unroll
-          for (int c = 0; c < BNT; ++c)
+          for (int c = 0; c < HB; ++c)
             if (n0 + c < out.N) pc[(long long)c * out.ldn] = out.alpha * acc[c];
         }
       }
-      const bool vec = inrow && out.ldn == 1 && n0 + BNT <= out.N &&
+      const bool vec = inrow && out.ldn == 1 && n0 + HB <= out.N &&
                        ((reinterpret_cast<uintptr_t>(out.C) & 15) == 0) &&
                        (out.out_f64 ? (out.ldm % 2 == 0) : (out.ldm % 4 == 0));
       if (inrow && !tstore) {
         const long long rowoff = (long long)gm * out.ldm;
 #pragma unroll
-        for (int c = 0; c < BNT; c += 4) {
+        for (int c = 0; c < HB; c += 4) {
           const float r0 = out.alpha * acc[c], r1 = out.alpha * acc[c + 1];
           const float r2 = out.alpha * acc[c + 2], r3 = out.alpha * acc[c + 3];
           if (vec) {

@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(RT) reduce_kernel(const T* __restrict__ x, con
   __shared__ bool last;
   double re = 0.0, im = 0.0;
   const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 4
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     if (MODE == 0) acc_dot<T>(x[i], y[i], re, im);
     else acc_dot<T>(x[i], x[i], re, im);
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(RT) multidot_partial(const T* __restrict__ Q, 
   const T* q = Q + (long long)j * ldq;
   double re = 0.0, im = 0.0;
   const long long stride = (long long)gridDim.x * blockDim.x;
+#pragma unroll 4
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) acc_dot<T>(q[i], w[i], re, im);
   block_sum2(re, im, sh);
   if (threadIdx.x == 0) {
@@ -260,12 +262,12 @@ int vfill_random(T* x, long long n, unsigned long long seed, cudaStream_t s) {
   return DMRG_OK;
 }
 
-// partial scratch needs 2*k*G doubles with G = grid_for(n)
+// partial scratch needs 2*k*G doubles with G = min(grid_for(n), MULTIDOT_MAX_GRID)
 template <typename T>
 int multidot_ws(const T* Q, long long ldq, int k, const T* w, long long n, T* h, double* partial, cudaStream_t s) {
   if (k <= 0) return DMRG_OK;
   int g = grid_for(n);
-  if (g > 64) g = 64;
+  if (g > MULTIDOT_MAX_GRID) g = MULTIDOT_MAX_GRID;
   dim3 grid(g, k);
   multidot_partial<T><<<grid, RT, 0, s>>>(Q, ldq, w, n, partial);
   DMRG_CHECK_LAUNCH();
