@@ -6,7 +6,8 @@
 // so y = X / sigma lies in [-1, 1], and cut into three 8-bit digits and a
 // tail:
 //   y = D0 + D1 + D2 + T,  D0 = d0 2^-7, D1 = d1 2^-15, D2 = d2 2^-23,
-//   |d0|, |d1|, |d2| <= 128 (integers),  |T| <= 2^-24,  T = Th + Tl (TF32).
+//   |d0|, |d1|, |d2| <= 128 (integers),  |T| <= 1.5 2^-24,  T = Th + Tl (TF32)
+// (the digits are those of y rounded to FP32, T holds the rest of y).
 // Every digit is exact in TF32 and every digit product is exact in FP32.
 // Per K-slice of 32 the products of one order are summed in their own TMEM
 // accumulator:
@@ -18,8 +19,8 @@
 // slices as int32 counts of their unit.  The tail
 //   P3 = sum over (D1 D2, D2 D1, D0 Th, Th D0, D0 Tl, Tl D0, D2 D2, D1 Th,
 //                  Th D1, D2 Th, Th D2, D1 Tl, Tl D1)
-// (products <= 2^-24) is summed in FP32; the pairs left out are below
-// 2^-47 per product.  Then
+// (products <= 1.5 2^-24) is summed in FP32; the pairs left out are below
+// 2^-46 per product.  Then
 //   G_ab = sigma_a sigma_b (P0 2^-14 + P1 2^-22 + P2 2^-30 + P3)
 // with the first three terms exact (45 bits, added exactly in FP64).
 // Against an extended-precision Gram the error is ~1e-13 relative to
@@ -73,13 +74,16 @@ __global__ void colmax_kernel(const double* __restrict__ X, long long ld, int m,
   __shared__ double sh[8][33];
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
-  double v = 0.0;
+  // |x| and its maximum on the bit patterns (integer compares order
+  // non-negative doubles like their values; no FP64 arithmetic)
+  unsigned long long v = 0ull;
   bool bad = false;
   if (c < k) {
     for (int r = blockIdx.y * 8 + ty; r < m; r += gridDim.y * 8) {
-      const double x = X[(long long)r * ld + c];
-      if (!isfinite(x)) bad = true;
-      v = fmax(v, fabs(x));
+      const unsigned long long a =
+          static_cast<unsigned long long>(__double_as_longlong(X[(long long)r * ld + c])) & 0x7FFFFFFFFFFFFFFFull;
+      if (a >= 0x7FF0000000000000ull) bad = true;   // inf or nan
+      v = a > v ? a : v;
     }
   }
   if (bad) atomicExch(err, DMRG_ERR_NAN);
@@ -87,9 +91,8 @@ __global__ void colmax_kernel(const double* __restrict__ X, long long ld, int m,
   __syncthreads();
   if (ty == 0 && c < k) {
 #pragma unroll
-    for (int j = 1; j < 8; ++j) v = fmax(v, sh[j][lane]);
-    // max of non-negative doubles through their bit patterns
-    atomicMax(&mx[c], static_cast<unsigned long long>(__double_as_longlong(v)));
+    for (int j = 1; j < 8; ++j) v = sh[j][lane] > v ? sh[j][lane] : v;
+    atomicMax(&mx[c], v);
   }
 }
 
@@ -124,21 +127,33 @@ __global__ void digits_kernel(const double* __restrict__ X, long long ld, int m,
     if (c >= k || r >= Kp) continue;
     const double sg = pow2_ceil(__longlong_as_double(static_cast<long long>(mx[c])));
     if (r == 0) sigma[c] = sg;
-    // every step below is exact in FP64: scaling by powers of two, rounding
-    // to an integer, and the difference of a number and its rounding
-    const double y = t[tx][j] * (1.0 / sg);
-    const double d0 = rint(y * 128.0);
-    const double r1 = y * 128.0 - d0;             // |r1| <= 1/2
-    const double d1 = rint(r1 * 256.0);
-    const double r2 = r1 * 256.0 - d1;
-    const double d2 = rint(r2 * 256.0);
-    const double tt = (r2 * 256.0 - d2) * 0x1p-23;   // |tt| <= 2^-24
-    const float th = to_tf32(static_cast<float>(tt));
-    const float tl = to_tf32(static_cast<float>(tt - static_cast<double>(th)));
+    // y = x / sg (|y| <= 1) as an FP32 pair yh + yl (48 bits; one FP64
+    // product and one subtraction, the rest bit operations and FP32
+    // arithmetic: GB300's FP64 pipe bounded the all-FP64 form).  The digits come from yh: every FP32
+    // step below is exact (power-of-two scalings, integer rounding, and the
+    // difference of a number and its rounding), so Z = yh 2^23 =
+    // d0 2^16 + d1 2^8 + d2 + rem exactly with |d*| <= 128, |rem| <= 1/2.
+    // 1/sg from the exponent bits (sg = 2^(e - 1023), 1 <= e <= 2045 after
+    // pow2_ceil: 1/sg = 2^(1023 - e), biased exponent 2046 - e)
+    const int e = (int)((static_cast<unsigned long long>(__double_as_longlong(sg)) >> 52) & 0x7FF);
+    const double inv = (e >= 1 && e <= 2045)
+                           ? __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(2046 - e) << 52))
+                           : 1.0 / sg;
+    const double y = t[tx][j] * inv;      // exact: a power-of-two scaling
+    const float yh = narrow(y);
+    const float yl = narrow(y - widen(yh));   // exact difference
+    const float d0 = rintf(yh * 128.0f);
+    const float r1 = yh * 128.0f - d0;
+    const float d1 = rintf(r1 * 256.0f);
+    const float r2 = r1 * 256.0f - d1;
+    const float d2 = rintf(r2 * 256.0f);
+    const float tt = fmaf(r2 * 256.0f - d2, 0x1p-23f, yl);   // tail of y beyond the digits, |tt| <= 1.5 2^-24
+    const float th = to_tf32(tt);
+    const float tl = to_tf32(tt - th);
     const long long o = (long long)c * Kp + r;
-    D0[o] = static_cast<float>(d0 * 0x1p-7);
-    D1[o] = static_cast<float>(d1 * 0x1p-15);
-    D2[o] = static_cast<float>(d2 * 0x1p-23);
+    D0[o] = d0 * 0x1p-7f;
+    D1[o] = d1 * 0x1p-15f;
+    D2[o] = d2 * 0x1p-23f;
     Th[o] = th;
     Tl[o] = tl;
   }

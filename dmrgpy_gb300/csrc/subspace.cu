@@ -135,20 +135,26 @@ __global__ void scale_perturb_kernel(double* __restrict__ Z, long long ld, int k
   if (c >= k) return;
   const long long i = (long long)r * k + c;
   double* z = Z + (long long)r * ld + c;
-  *z = *z * f[c] + eps * static_cast<double>(hash_uniform(seed, i));
+  // FP64 as the column norms: with both in FP32 one ill-conditioned case
+  // (a half-random start, tests/test_gpu_truncation.py) no longer converged
+  // within the step limit.  The draw is widened from its bit pattern.
+  *z = fma(*z, f[c], eps * widen(hash_uniform(seed, i)));
 }
 
-// n2[c] = sum_r Z[r][c]^2: one block per 32 columns, 32 row lanes per
-// column (coalesced 256-byte row segments), partial sums combined in shared
-// memory in a fixed order (deterministic)
+// part[y][c] = sum of Z[r][c]^2 over the rows of chunk y (rows 32 y + ty +
+// 32 gridDim.y j for row lane ty): blocks of 32 columns x 32 row lanes
+// (coalesced 256-byte row segments), gridDim.y row chunks so that 1024
+// columns spread over 4 x 32 SMs; lanes combined in shared memory in a
+// fixed order (deterministic)
+constexpr int COLSQ_CHUNKS = 4;
 __global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ Z, long long ld, int m, int k,
-                                                     double* __restrict__ n2) {
+                                                     double* __restrict__ part) {
   __shared__ double sh[32][33];
   const int lane = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
   double s = 0.0;
   if (c < k)
-    for (int r = ty; r < m; r += 32) {
+    for (int r = blockIdx.y * 32 + ty; r < m; r += 32 * gridDim.y) {
       const double z = Z[(long long)r * ld + c];
       s = fma(z, z, s);
     }
@@ -157,19 +163,30 @@ __global__ void __launch_bounds__(1024) colsq_kernel(const double* __restrict__ 
   if (ty == 0 && c < k) {
     double t = 0.0;
     for (int j = 0; j < 32; ++j) t += sh[j][lane];
-    n2[c] = t;
+    part[(long long)blockIdx.y * k + c] = t;
   }
 }
 
-// B = b*A + c*I  (k x k), also reports max|A - I| into *dev.  A block
-// covers POLY_ROWS whole rows, so the grid ends in k / POLY_ROWS atomics on
-// *dev (one per block), not one per 256 elements; one row per block gives
-// k blocks, enough to spread a 1024 x 1024 matrix over every SM.
-constexpr int POLY_ROWS = 1;
+// n2[c] = sum of the chunk partials, in chunk order
+__global__ void colsq_sum_kernel(const double* __restrict__ part, int chunks, int k, double* __restrict__ n2) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  double t = 0.0;
+  for (int y = 0; y < chunks; ++y) t += part[(long long)y * k + c];
+  n2[c] = t;
+}
+
+// B = b*A + c*I  (k x k), also reports max|A - I| into *dev.  Blocks walk
+// whole rows (row r = blockIdx.y + j gridDim.y); the grid is two blocks per
+// SM, so it ends in at most POLY_BLOCKS atomics on *dev (one per block):
+// one block per row of a 1024 x 1024 matrix spent ~10 us in serialised
+// atomics.
+constexpr int POLY_BLOCKS = 2 * 152;
+inline dim3 poly_grid(int k) { return dim3(1, k < POLY_BLOCKS ? k : POLY_BLOCKS); }
 __global__ void poly_kernel(const double* __restrict__ A, int k, double b, double c, double* __restrict__ B,
                             unsigned long long* __restrict__ dev) {
   double mx = 0.0;
-  for (int r = blockIdx.y * POLY_ROWS; r < k && r < (blockIdx.y + 1) * POLY_ROWS; ++r)
+  for (int r = blockIdx.y; r < k; r += gridDim.y)
     for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
       const long long i = (long long)r * k + cc;
       const double a = A[i];
@@ -207,17 +224,18 @@ __device__ __forceinline__ void split_h(float x, float scale, __half& hi, __half
 __global__ void poly_split_kernel(const double* __restrict__ A, int k, double b, double c, double scale,
                                   __half* __restrict__ hi, __half* __restrict__ lo, int Kk,
                                   unsigned long long* __restrict__ dev) {
-  // POLY_ROWS whole rows per block (one atomic per block); FP32 arithmetic
-  // (A carries the FP32-level accuracy of the split products)
+  // whole rows per block as in poly_kernel (one atomic per block); FP32
+  // arithmetic (A carries the FP32-level accuracy of the split products)
   const float bf = static_cast<float>(b), cf = static_cast<float>(c), sf = static_cast<float>(scale);
-  double mx = 0.0;
-  for (int r = blockIdx.y * POLY_ROWS; r < k && r < (blockIdx.y + 1) * POLY_ROWS; ++r)
+  float mxf = 0.f;
+  for (int r = blockIdx.y; r < k; r += gridDim.y)
     for (int cc = threadIdx.x; cc < k; cc += blockDim.x) {
       const float a = narrow(A[(long long)r * k + cc]);
       split_h(fmaf(bf, a, r == cc ? cf : 0.f), sf, hi[(long long)r * Kk + cc], lo[(long long)r * Kk + cc]);
       const float dv = fabsf(a - (r == cc ? 1.f : 0.f));
-      if (!(dv <= mx)) mx = dv == dv ? static_cast<double>(dv) : INFINITY;   // a non-finite entry reports +inf
+      if (!(dv <= mxf)) mxf = dv == dv ? dv : INFINITY;   // a non-finite entry reports +inf
     }
+  double mx = mxf;
   __shared__ double red[32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -330,7 +348,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
   if (st == DMRG_ERR_ARG || st == DMRG_ERR_WORKSPACE) DMRG_TRY(tgemm_gram(Z, ld, m, k, A, s));
   else DMRG_TRY(st);
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
+  poly_kernel<<<poly_grid(k), 256, 0, s>>>(A, k, -0.5, 0.5, B, dev);
   DMRG_CHECK_LAUNCH();
   return tf32x3_gemm_ex(0, 0, m, k, k, 1.f, Z, ld, B, k, 1, Z, ld, gw, err, s);
 }
@@ -338,7 +356,7 @@ int orth_fp64_correct(double* Z, long long ld, int m, int k, double* A, double* 
 // max|A - I| of a k x k Gram matrix (host value; synchronises the stream)
 int gram_deviation(const double* A, int k, double* B, unsigned long long* dev, double* out, cudaStream_t s) {
   DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-  poly_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
+  poly_kernel<<<poly_grid(k), 256, 0, s>>>(A, k, 1.0, 0.0, B, dev);
   DMRG_CHECK_LAUNCH();
   unsigned long long h = 0;
   DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -371,7 +389,11 @@ int orth_polar(double* Z, long long ld, int m, int k, double* A, double* B, doub
   DMRG_TRY(gram_deviation(A, k, B, dev, &d0, s));
   if (d0 < 1e-5) return exact ? orth_fp64_correct(Z, ld, m, k, A, B, dev, gw, gw_bytes, err, s) : DMRG_OK;
   // column scaling: unit columns / sqrt(k)  (=> all singular values <= 1)
-  colsq_kernel<<<(k + 31) / 32, 1024, 0, s>>>(Z, ld, m, k, n2);
+  // the chunk partials go to B (k x k, free until the final correction)
+  const int chunks = k >= COLSQ_CHUNKS ? COLSQ_CHUNKS : 1;
+  colsq_kernel<<<dim3((k + 31) / 32, chunks), 1024, 0, s>>>(Z, ld, m, k, B);
+  DMRG_CHECK_LAUNCH();
+  colsq_sum_kernel<<<(k + 255) / 256, 256, 0, s>>>(B, chunks, k, n2);
   DMRG_CHECK_LAUNCH();
   col_factor_kernel<<<(k + 255) / 256, 256, 0, s>>>(n2, k, 1.0 / sqrt((double)k));
   DMRG_CHECK_LAUNCH();
@@ -403,7 +425,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* A, double* B, doub
       // step a X + b X A + c X A^2 as one product
       const double a = 3.4445, b = -4.7750, c = 2.0315;
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
+      poly_split_kernel<<<poly_grid(k), 256, 0, s>>>(A, k, c, b, SP, ps.ps_hi, ps.ps_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       GemmOut b2{};
       b2.C = nullptr; b2.M = k; b2.N = k; b2.out_f64 = 1; b2.alpha = (float)(1.0 / (SA * SP)); b2.diag = a;
@@ -412,7 +434,7 @@ int orth_polar(double* Z, long long ld, int m, int k, double* A, double* B, doub
     } else {
       // convergence check on A, then X <- X (1.5 I - 0.5 A)
       DMRG_CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(unsigned long long), s));
-      poly_split_kernel<<<dim3(1, (k + POLY_ROWS - 1) / POLY_ROWS), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
+      poly_split_kernel<<<poly_grid(k), 256, 0, s>>>(A, k, -0.5, 1.5, SB, ps.bs_hi, ps.bs_lo, Kk, dev);
       DMRG_CHECK_LAUNCH();
       unsigned long long h = 0;
       DMRG_CUDA_TRY(cudaMemcpyAsync(&h, dev, sizeof(h), cudaMemcpyDeviceToHost, s));

@@ -23,25 +23,37 @@ def _tf32(x):
 
 
 def _digits(X):
+    """As digits_kernel: y = X / sigma as the FP32 pair yh + yl; the digits
+    are those of yh (every FP32 step exact), the tail is the digits'
+    remainder plus yl, rounded once to FP32 and split into a TF32 pair."""
     mx = np.abs(X).max(axis=0)
     sigma = np.where(mx > 0, 2.0 ** np.ceil(np.log2(np.where(mx > 0, mx, 1.0))), 1.0)
     y = X / sigma
-    d0 = np.rint(y * 128)
-    r1 = y * 128 - d0
-    d1 = np.rint(r1 * 256)
-    r2 = r1 * 256 - d1
-    d2 = np.rint(r2 * 256)
-    tt = (r2 * 256 - d2) * 2.0 ** -23
-    th = _tf32(tt.astype(np.float32)).astype(np.float64)
-    tl = _tf32((tt - th).astype(np.float32)).astype(np.float64)
-    return sigma, [d0 / 128, d1 * 2.0 ** -15, d2 * 2.0 ** -23, th, tl], (d0, d1, d2, tt)
+    yh = y.astype(np.float32)
+    yl = (y - yh.astype(np.float64)).astype(np.float32)
+    f = np.float32
+    d0 = np.rint(yh * f(128))
+    r1 = yh * f(128) - d0
+    d1 = np.rint(r1 * f(256))
+    r2 = r1 * f(256) - d1
+    d2 = np.rint(r2 * f(256))
+    rem = r2 * f(256) - d2
+    # the FP32 steps were exact: yh 2^23 = d0 2^16 + d1 2^8 + d2 + rem
+    assert np.array_equal(yh.astype(np.float64) * 2.0 ** 23,
+                          d0.astype(np.float64) * 2.0 ** 16 + d1.astype(np.float64) * 2.0 ** 8 + d2 + rem)
+    tt = (rem.astype(np.float64) * 2.0 ** -23 + yl.astype(np.float64)).astype(np.float32)
+    th = _tf32(tt)
+    tl = _tf32(tt - th)
+    D = [d0.astype(np.float64) / 128, d1.astype(np.float64) * 2.0 ** -15, d2.astype(np.float64) * 2.0 ** -23,
+         th.astype(np.float64), tl.astype(np.float64)]
+    return sigma, D, (d0, d1, d2, tt.astype(np.float64))
 
 
 def _gram_model(X):
     m, k = X.shape
     sigma, D, (d0, d1, d2, tt) = _digits(X)
     assert max(np.abs(d0).max(), np.abs(d1).max(), np.abs(d2).max()) <= 128
-    assert np.abs(tt).max() <= 2.0 ** -24
+    assert np.abs(tt).max() <= 1.5 * 2.0 ** -24
     acc = [np.zeros((k, k), np.int64) for _ in range(3)]
     tail = np.zeros((k, k), np.float32)
     units = (2.0 ** 14, 2.0 ** 22, 2.0 ** 30)
