@@ -52,6 +52,7 @@ def main(argv=None):
     ap.add_argument("--sweeps", type=int, default=8)
     ap.add_argument("--fd-sweeps", type=int, default=3)
     ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--no-gradients", action="store_true", help="sweeps only (no adjoint or finite differences)")
     args = ap.parse_args(argv)
     n, C = args.n, args.chains
     rng = np.random.default_rng(args.seed)
@@ -75,6 +76,19 @@ def main(argv=None):
         print(json.dumps({"sweep": sw + 1, "s": times[-1], "energy_per_site_min": float(e.min()),
                           "energy_per_site_max": float(e.max())}), flush=True)
     energies = np.asarray(energies, dtype=np.float64)
+    out = {
+        "workload": "%d TFIM chains, N=%d, J=1, h~U[0.5,1.5], chi_max~{16,32,64,128}, batched two-site DMRG "
+                    "(grouped launches, graph-replayed Lanczos), FP64" % (C, n),
+        "sweeps": args.sweeps,
+        "s_per_sweep_last": times[-1],
+        "s_per_sweep_first": times[0],
+        "bond_updates_per_s": C * 2 * (n - 1) / times[-1],
+        "energy_per_site_min": float((energies / n).min()),
+        "energy_per_site_max": float((energies / n).max()),
+    }
+    if args.no_gradients:
+        print(json.dumps(out))
+        return
 
     # dE/dh by the adjoint pass, and <dH/dh> = sum_i <Sx_i> on the state
     from .engine import Engine
@@ -107,22 +121,14 @@ def main(argv=None):
     fd = (e_pm[0] - e_pm[1]) / (2 * dh)
 
     scale = np.maximum(1.0, np.abs(dedh))
-    out = {
-        "workload": "%d TFIM chains, N=%d, J=1, h~U[0.5,1.5], chi_max~{16,32,64,128}, batched two-site DMRG "
-                    "(grouped launches, graph-replayed Lanczos), FP64" % (C, n),
-        "sweeps": args.sweeps,
-        "s_per_sweep_last": times[-1],
-        "s_per_sweep_first": times[0],
-        "bond_updates_per_s": C * 2 * (n - 1) / times[-1],
-        "energy_per_site_min": float((energies / n).min()),
-        "energy_per_site_max": float((energies / n).max()),
+    out.update({
         "gradient_s": t_grad,
         "max_rel_adjoint_vs_expectation": float(np.max(np.abs(dedh - sx) / scale)),
         "max_rel_adjoint_vs_fd": float(np.max(np.abs(dedh - fd) / scale)),
         "median_rel_adjoint_vs_fd": float(np.median(np.abs(dedh - fd) / scale)),
         "fd_dh": dh,
         "fd_sweeps": args.fd_sweeps,
-    }
+    })
     print(json.dumps(out))
 
 
