@@ -18,11 +18,15 @@ Prints one JSON line per sweep (seconds, energy per site range), then one
 summary line: seconds per lock-step sweep, bond updates per second, the
 energy per site range and the largest disagreements of the gradients.
 
-On one GB300 the full-size run (256 chains, N = 64, 8 sweeps) did not finish
-within 480 s (that run printed only the final summary, so no per-sweep time
-was kept).  The likely bound: the batched truncation factorises each
-chain's two-site tensor with the one-CTA FP64 Jacobi SVD, which at a bond
-cap of 128 (256 x 256 tensors) runs on a single SM's FP64 pipe.
+Measured on one GB300 (`--sweeps 2 --no-gradients`): 9.6 s for the first
+lock-step sweep and 12.4 s for the second (bonds at their caps), i.e. 2,600
+bond updates per second over the 256 chains, ~95 ms per bond step of all
+chains.  The likely bound of a bond step: the batched truncation factorises
+each chain's two-site tensor with the one-CTA FP64 Jacobi SVD, which at a
+bond cap of 128 (256 x 256 tensors) runs on a single SM's FP64 pipe.  The
+full run with gradients (8 sweeps, 256 adjoint passes driven chain by chain
+from the host, 2 x 3 finite-difference sweeps) did not finish within 480 s;
+its parts were not timed separately.
 """
 import argparse
 import json
